@@ -1,0 +1,387 @@
+"""Benchmark: 30-qubit complex64 state, 1,000 random gates, one kernel per
+gate -- algorithmic HBM GB/s and fraction of the measured copy peak.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One step = the whole 1,000-gate circuit (canonical generator, seed 0) from
+|0...0> over the 8 GiB state.  Algorithmic bytes = 2 x 8 B x 2^30 per gate
+(each amplitude read once and written once).  The state is 64x larger than
+L2, so no flush is needed between steps.
+
+value:   device-timed (CUDA events around the timed steps), state resident.
+e2e:     the same metric through the public functional API
+         (qcware_unitair_gb300.apply_operator) with the initial state copied
+         from pinned host memory and the final state copied back inside
+         the timed region.
+roofline: dense gate kernel, per-launch CUDA-event durations.
+cpu_baseline / --impl reference: the oracle's complex64 C port of the
+         reference path (OpenMP, all host threads) on the first gates of
+         the same circuit.
+Multi-GPU: replicas only (each rank runs its own state), scaling "weak".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+METRIC = "30q c64 HBM GB/s & %peak; served circuits/s, p50/p99 vs plain " \
+         "per-gate path"
+WORKLOAD = ("{n}-qubit complex64 state from |0...0>, {g} random "
+            "gates from {H,X,Y,Z,S,T,RX,RY,RZ,CNOT,CZ,SWAP}, one kernel per "
+            "gate")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--qubits", type=int, default=30)
+    p.add_argument("--gates", type=int, default=1000)
+    p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--cpu-seconds", type=float, default=15.0,
+                   help="budget of the CPU baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def peaks():
+    f = REPO / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """Per-launch DRAM bytes of the dense gate kernel from the committed ncu
+    summary (a `traffic_bytes_per_launch = N` line), or None."""
+    f = REPO / "profiles" / "dense_gate_30q_c64.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.strip().startswith("traffic_bytes_per_launch"):
+            try:
+                return float(line.split("=")[1].split()[0])
+            except (IndexError, ValueError):
+                return None
+    return None
+
+
+# ----------------------------------------------------------- distributed --
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def max_over_ranks(value: float, backend_device=None) -> float:
+    """Max of a float across ranks (identity without a process group)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return value
+    t = torch.tensor([value], dtype=torch.float64,
+                     device=backend_device or "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier():
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+
+
+# ---------------------------------------------------------------- clocks --
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons while timing."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = Path(f"/tmp/gbsv_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}",
+                 f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
+                    "note": "nvidia-smi unavailable"}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        self.path.unlink(missing_ok=True)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
+                    "note": "no samples"}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------- CPU baseline --
+def cpu_sample(n: int, gates, budget_s: float):
+    """Time the oracle's complex64 port (all host threads) on the first gates
+    of the circuit, in place on an n-qubit state, until budget_s passes."""
+    import numpy as np
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    psi = np.zeros(2 ** n, dtype=np.complex64)
+    psi[0] = 1
+    done, t0 = 0, time.perf_counter()
+    L = O.lib()
+    import ctypes
+    for g in gates:
+        m = np.ascontiguousarray(g.matrix().astype(np.complex64))
+        q = (ctypes.c_int * len(g.qubits))(*g.qubits)
+        rc = L.oracle_apply_c64(psi.ctypes.data, psi.ctypes.data, 1, n, 0,
+                                m.ctypes.data, 0, q, len(g.qubits))
+        if rc:
+            raise RuntimeError("oracle rejected a gate")
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    gbs = done * 2 * 8 * 2 ** n / dt / 1e9
+    return {"value": gbs, "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": f"first {done} gates of the {n}-qubit circuit, "
+                      f"in place, {dt:.1f} s",
+            "s_per_gate": dt / done}
+
+
+# -------------------------------------------------------------- GPU arm ---
+def run_gpu(args, ws, rank, local):
+    import numpy as np
+    import torch
+
+    import qcware_unitair_gb300 as ug
+    from qcware_unitair_gb300 import _lib
+    from qcware_unitair_gb300.circuits import random_circuit
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    n, G = args.qubits, args.gates
+    gates = random_circuit(n, G, seed=args.seed)
+    N = 2 ** n
+    bytes_per_gate = 2 * 8 * N
+    mats_host = [torch.from_numpy(g.matrix()).to(torch.complex64)
+                 for g in gates]
+    mats = [m.to(dev) for m in mats_host]
+    psi = torch.zeros(N, dtype=torch.complex64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step(record=None):
+        psi.zero_()
+        psi[0] = 1
+        for g, m in zip(gates, mats):
+            if record is not None:
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                ug.apply_operator_(m, g.qubits, psi)
+                e1.record(stream)
+                record.append((e0, e1))
+            else:
+                ug.apply_operator_(m, g.qubits, psi)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    events = []
+    l0 = _lib.launch_count()
+    with ClockSampler(local) as clocks:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(args.steps):
+            step(events)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    launches = _lib.launch_count() - l0
+    ms = t0.elapsed_time(t1)
+    ms = max_over_ranks(ms, dev)
+    per_launch_ms = [a.elapsed_time(b) for a, b in events]
+    # psi.zero_ / psi[0] = 1 are torch fills between circuits: not our kernels
+    gate_ms = statistics.mean(per_launch_ms)
+    total_bytes = bytes_per_gate * G * args.steps * ws
+    value = total_bytes / (ms / 1e3) / 1e9
+
+    # ---- e2e through the public functional API, host buffers -----------
+    host_in = torch.zeros(N, dtype=torch.complex64, pin_memory=True)
+    host_in[0] = 1
+    host_out = torch.empty(N, dtype=torch.complex64, pin_memory=True)
+    mats_pinned = [m.pin_memory() for m in mats_host]
+    del psi
+    torch.cuda.empty_cache()
+
+    def e2e_step():
+        state = host_in.to(dev, non_blocking=True)
+        ops = [m.to(dev, non_blocking=True) for m in mats_pinned]
+        for g, m in zip(gates, ops):
+            state = ug.apply_operator(m, g.qubits, state)
+        host_out.copy_(state, non_blocking=True)
+        return state
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    e2e_steps = max(1, min(args.steps, 2))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dev)
+    e2e_value = bytes_per_gate * G * e2e_steps * ws / e2e_s / 1e9
+    h2d = N * 8 + sum(m.numel() * 8 for m in mats_host)
+    d2h = N * 8
+    # final state sanity: unit norm
+    drift = abs(float(np.sum(np.abs(host_out.numpy().astype(np.complex128))
+                             ** 2)) - 1.0)
+
+    peak, peak_kind = peaks()
+    achieved = bytes_per_gate / (gate_ms / 1e3) / 1e9
+    traffic = profile_traffic()
+    result = {
+        "metric": METRIC, "value": round(value, 1), "unit": "GB/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+        "data": "synthetic: canonical random circuit (numpy seed "
+                f"{args.seed}) applied to |0...0>",
+        "config": {"workload": WORKLOAD.format(n=n, g=G), "qubits": n, "gates": G,
+                   "state_bytes": N * 8,
+                   "l2": "inputs larger than L2 (8 GiB state vs 129 MB L2); "
+                         "no flush",
+                   "parallelism": f"replicas x{ws}"},
+        "pct_of_peak": round(100 * value / peak, 1),
+        "amp_updates_per_s": N * G * args.steps * ws / (ms / 1e3),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4),
+                     "peak_source": peak_kind,
+                     "kernel": "dense_chunk_kernel (1- and 2-qubit gates)",
+                     "traffic": traffic,
+                     "algorithmic_bytes_per_launch": bytes_per_gate,
+                     "launch_ms_mean": round(gate_ms, 4),
+                     "launch_ms_p50": round(statistics.median(per_launch_ms),
+                                            4),
+                     "launch_ms_max": round(max(per_launch_ms), 4)},
+        "e2e": {"value": round(e2e_value, 1), "unit": "GB/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "api": "qcware_unitair_gb300.apply_operator (functional)",
+                "final_norm_drift": drift},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_sample(n, gates, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def run_reference(args, ws, rank):
+    """Reference arm: the oracle's C port of the reference path (complex64
+    arithmetic, OpenMP over all host threads); each step is a bounded sample
+    of the same circuit.  Under torchrun only rank 0 runs."""
+    if rank != 0:
+        return
+    from qcware_unitair_gb300.circuits import random_circuit
+    n, G = args.qubits, args.gates
+    gates = random_circuit(n, G, seed=args.seed)
+    budget = max(2.0, args.cpu_seconds / max(1, args.steps + args.warmup))
+    for _ in range(args.warmup):
+        cpu_sample(n, gates, budget)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_sample(n, gates, budget))
+    elapsed = time.perf_counter() - t0
+    v = statistics.mean(x["value"] for x in vals)
+    result = {
+        "metric": METRIC, "value": round(v, 3), "unit": "GB/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * elapsed / args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64", "impl": "reference",
+        "data": "synthetic: canonical random circuit (numpy seed "
+                f"{args.seed}) applied to |0...0>",
+        "config": {"workload": WORKLOAD.format(n=n, g=G), "qubits": n, "gates": G,
+                   "parallelism": "host threads"},
+        "cpu_baseline": {"value": round(v, 3), "unit": "GB/s",
+                         "cores": vals[0]["cores"], "kind": "port",
+                         "sample": vals[0]["sample"]},
+        "e2e": {"value": round(v, 3), "unit": "GB/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(result), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    run_gpu(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,177 @@
+/*
+ * gbsv.h -- C ABI of the GB300 state-vector engine (libgbsv.so).
+ *
+ * Every entry point takes raw device pointers, plain sizes and a
+ * cudaStream_t passed as void*, returns an int status (GBSV_OK == 0) and
+ * never allocates or frees caller memory.  Nothing here names a torch type;
+ * a ctypes / cffi binding is all a Python caller needs.
+ *
+ * Layout contract (identical to unitair's "vector layout"):
+ *   - a state is 2^n complex amplitudes, contiguous, interleaved (re, im);
+ *     complex64 = 2 x float, complex128 = 2 x double;
+ *   - qubit 0 is the MOST significant bit of the amplitude index, i.e.
+ *     qubit q has stride 2^(n-1-q) amplitudes
+ *     (unitair: src/unitair/states/conversions.py:5-45, tensor layout is a
+ *     C-order view of the last dim as (2,...,2));
+ *   - a k-qubit operator is a row-major 2^k x 2^k complex matrix whose row
+ *     and column index is sum_j b_{q_j} 2^(k-1-j) for qubits = (q_0..q_{k-1}),
+ *     so the first listed qubit is the matrix MSB
+ *     (unitair: src/unitair/simulation/operations.py:151-186 and :322);
+ *   - out[a] = sum_b op[a, b] * in[b]  (no conjugation).
+ *
+ * Batches: num_states states are processed; state s is read at
+ * in + s * in_stride (in_stride == 0 broadcasts one state to every output,
+ * unitair's "operator batched, state unbatched" case,
+ * operations.py:304-309) and written densely at out + s * 2^n.  Operator s
+ * is read at ops + s * op_stride complex elements (0 = one shared operator).
+ * Any other broadcast that unitair accepts is reduced to these two strides
+ * by the host layer before the call.
+ *
+ * In-place use (in == out) is allowed for every apply entry point whose
+ * in_stride is 2^n: each amplitude group is read and written by the same
+ * thread.
+ */
+#ifndef GBSV_H
+#define GBSV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define GBSV_OK 0
+#define GBSV_ERR_INVALID_ARG 1   /* bad size, qubit index, dtype or stride */
+#define GBSV_ERR_UNSUPPORTED 2   /* valid request outside this build's limits */
+#define GBSV_ERR_CUDA 3          /* a CUDA runtime call failed */
+#define GBSV_ERR_SCRATCH 4       /* scratch buffer missing or too small */
+#define GBSV_ERR_TIMEOUT 5       /* a bounded device-side wait gave up */
+
+/* ---- element types ---------------------------------------------------- */
+#define GBSV_C64 0    /* complex64: float re, float im */
+#define GBSV_C128 1   /* complex128: double re, double im */
+#define GBSV_F32 2    /* real float32 (angles, diagonals, probabilities) */
+#define GBSV_F64 3    /* real float64 */
+
+#define GBSV_MAX_DIMS 8
+#define GBSV_MAX_DENSE_QUBITS 12
+
+/* Broadcast descriptor for batched reductions and elementwise ops: the
+ * output has shape[0..ndim-1]; operand a (b) element at multi-index i is
+ * at sum_d i[d] * stride_a[d] (stride_b[d]); a zero stride broadcasts. */
+typedef struct gbsv_bcast {
+  int32_t ndim;
+  int32_t pad_;
+  int64_t shape[GBSV_MAX_DIMS];
+  int64_t stride_a[GBSV_MAX_DIMS];
+  int64_t stride_b[GBSV_MAX_DIMS];
+} gbsv_bcast_t;
+
+/* ---- library information --------------------------------------------- */
+int gbsv_abi_version(void);
+const char* gbsv_status_string(int status);
+/* Text of the last CUDA or argument error seen by this thread. */
+const char* gbsv_last_error(void);
+/* Number of kernels this library has launched in this process. */
+uint64_t gbsv_launch_count(void);
+
+/* ---- gate application ------------------------------------------------- */
+
+/* Apply a dense k-qubit operator (0 <= k <= GBSV_MAX_DENSE_QUBITS) to the
+ * listed qubits of every state.  Replaces unitair.simulation.apply_operator
+ * (src/unitair/simulation/operations.py:45-148) together with
+ * apply_operator_tensor (:151-186) and act_first_qubits_tensor (:258-329):
+ * the permute -> einsum -> permute sequence becomes one pass that addresses
+ * amplitude pairs / quads by bit insertion.  qubits is a HOST array. */
+int gbsv_apply_operator(const void* state_in, void* state_out, int dtype,
+                        int num_qubits, int64_t num_states, int64_t in_stride,
+                        const void* ops, int64_t op_stride,
+                        const int32_t* qubits, int num_targets, void* stream);
+
+/* Apply a 2x2 operator to every qubit.  Replaces
+ * unitair.simulation.apply_all_qubits (operations.py:332-413).  With
+ * op_qubit_stride == 0 the same operator (per state) acts on all qubits,
+ * as in unitair; a non-zero op_qubit_stride (complex elements) reads a
+ * separate operator for qubit q at ops + s*op_stride + q*op_qubit_stride
+ * (an extension: unitair rejects per-qubit operator batches). */
+int gbsv_apply_all_qubits(const void* state_in, void* state_out, int dtype,
+                          int num_qubits, int64_t num_states,
+                          int64_t in_stride, const void* ops,
+                          int64_t op_stride, int64_t op_qubit_stride,
+                          void* stream);
+
+/* out = exp(-i * angles) * state with broadcasting.  Replaces
+ * unitair.simulation.apply_phase (operations.py:15-42).  bc describes the
+ * output shape; operand a is the real angle tensor (angle_dtype GBSV_F32 or
+ * GBSV_F64), operand b the state (state_dtype GBSV_C64 / GBSV_C128); out is
+ * dense in out_dtype (GBSV_C64 / GBSV_C128, torch's promotion result). */
+int gbsv_apply_phase(const void* angles, int angle_dtype, const void* state,
+                     int state_dtype, void* out, int out_dtype,
+                     const gbsv_bcast_t* bc, void* stream);
+
+/* ---- gradients --------------------------------------------------------- */
+
+/* Scratch bytes gbsv_operator_grad needs (0 = none). */
+size_t gbsv_operator_grad_scratch_bytes(int64_t num_states, int num_qubits,
+                                        int num_targets, int shared);
+
+/* dL/dU for out = U psi applied on `qubits` (torch's convention
+ * grad_U = grad_out psi^H, summed over the non-target qubits):
+ *   grad_ops[s][a, c] = sum_rest grad_out_s[rest|a] * conj(psi_s[rest|c]).
+ * shared != 0 sums over all states into one matrix (the operator was shared
+ * by the batch).  num_targets <= 6.  This is the operator half of the
+ * autograd backward that unitair gets from torch through its einsum
+ * (src/unitair/simulation/operations.py:322); the state half is
+ * gbsv_apply_operator with the conjugate-transposed operator. */
+int gbsv_operator_grad(const void* grad_out, const void* state_in, int dtype,
+                       int num_qubits, int64_t num_states, int64_t in_stride,
+                       const int32_t* qubits, int num_targets,
+                       void* grad_ops, int shared, void* scratch,
+                       size_t scratch_bytes, void* stream);
+
+/* ---- reductions (FP64 accumulation) ----------------------------------- */
+
+/* Scratch bytes a reduction over num_rows rows of length dim needs; 0 means
+ * the reduction runs in one kernel without scratch. */
+size_t gbsv_reduce_scratch_bytes(int64_t num_rows, int64_t dim);
+
+/* sum_i |state[r, i]|^2 for every row r.  Replaces
+ * unitair.states.norm_squared (src/unitair/states/innerprod.py:29-46).
+ * out_dtype GBSV_F32 / GBSV_F64 (the engine always accumulates in FP64). */
+int gbsv_norm_squared(const void* state, int dtype, int64_t num_rows,
+                      int64_t dim, void* out, int out_dtype, void* scratch,
+                      size_t scratch_bytes, void* stream);
+
+/* |state[i]|^2 elementwise; out is real of the state's precision.
+ * Replaces unitair.states.abs_squared (innerprod.py:4-26). */
+int gbsv_abs_squared(const void* state, int dtype, int64_t count, void* out,
+                     void* stream);
+
+/* sum_i conj(a[r, i]) * b[r, i] over broadcast rows (bc: row shape and row
+ * strides in units of rows of length dim; inner strides are 0 or 1).
+ * Replaces unitair.states.inner_product (innerprod.py:62-65).  out_dtype
+ * GBSV_C64 / GBSV_C128. */
+int gbsv_inner_product(const void* a, const void* b, int dtype,
+                       const gbsv_bcast_t* bc, int64_t dim,
+                       int64_t inner_stride_a, int64_t inner_stride_b,
+                       void* out, int out_dtype, void* scratch,
+                       size_t scratch_bytes, void* stream);
+
+/* sum_i diag[r, i] * |state[r, i]|^2 over broadcast rows (operand a = diag,
+ * b = state).  Replaces unitair.states.diag_expectation_value
+ * (innerprod.py:49-59).  out_dtype GBSV_F32 / GBSV_F64. */
+int gbsv_diag_expectation(const void* diag, int diag_dtype,
+                          const void* state, int state_dtype,
+                          const gbsv_bcast_t* bc, int64_t dim,
+                          int64_t inner_stride_diag,
+                          int64_t inner_stride_state, void* out,
+                          int out_dtype, void* scratch, size_t scratch_bytes,
+                          void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBSV_H */

@@ -1,0 +1,21 @@
+"""qcware_unitair_gb300 -- a GB300-native state-vector engine.
+
+Drop-in for unitair's hot path: ``simulation.apply_operator``,
+``apply_all_qubits``, ``apply_phase`` and the ``states`` reductions, on the
+same torch tensors (vector layout, qubit 0 = most significant index bit,
+unitair's batch broadcasting).  Every operation is a hand-written sm_103a
+CUDA kernel reached through the C ABI in include/gbsv.h; CUDA tensors only.
+"""
+from . import gates, states, simulation, initializations  # noqa: F401
+from .states import (StateLayout, StateShapeError, count_qubits,  # noqa
+                     hilbert_space_dim, diag_expectation_value,
+                     inner_product, norm_squared, abs_squared)
+from .simulation import (apply_operator, apply_operator_, apply_all_qubits,  # noqa
+                         apply_each_qubit, apply_phase, act_first_qubits)
+from .initializations import (unit_vector, uniform_superposition,  # noqa
+                              rand_state)
+
+VECTOR_LAYOUT = StateLayout.VECTOR
+TENSOR_LAYOUT = StateLayout.TENSOR
+
+__version__ = "0.1.0"

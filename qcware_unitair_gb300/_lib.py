@@ -1,0 +1,117 @@
+"""ctypes binding of libgbsv.so, the C ABI declared in include/gbsv.h.
+
+The library is loaded from the in-tree build directory.  If it is missing
+the engine raises: there is no CPU or pure-torch fallback for any kernel.
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+
+from . import build_lib
+
+GBSV_OK = 0
+GBSV_ERR_INVALID_ARG = 1
+GBSV_ERR_UNSUPPORTED = 2
+GBSV_ERR_CUDA = 3
+GBSV_ERR_SCRATCH = 4
+GBSV_ERR_TIMEOUT = 5
+
+C64, C128, F32, F64 = 0, 1, 2, 3
+MAX_DIMS = 8
+MAX_DENSE_QUBITS = 12
+
+
+class GbsvError(RuntimeError):
+    """A libgbsv entry point returned a non-zero status."""
+
+    def __init__(self, status: int, what: str, detail: str):
+        self.status = status
+        super().__init__(f"{what}: {detail} (status {status})")
+
+
+class Bcast(ctypes.Structure):
+    _fields_ = [
+        ("ndim", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
+        ("shape", ctypes.c_int64 * MAX_DIMS),
+        ("stride_a", ctypes.c_int64 * MAX_DIMS),
+        ("stride_b", ctypes.c_int64 * MAX_DIMS),
+    ]
+
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_I32 = ctypes.c_int32
+_I64 = ctypes.c_int64
+_SZ = ctypes.c_size_t
+_BC = ctypes.POINTER(Bcast)
+
+# name -> (restype, argtypes); must match include/gbsv.h exactly.
+SIGNATURES = {
+    "gbsv_abi_version": (_I, []),
+    "gbsv_status_string": (ctypes.c_char_p, [_I]),
+    "gbsv_last_error": (ctypes.c_char_p, []),
+    "gbsv_launch_count": (ctypes.c_uint64, []),
+    "gbsv_apply_operator": (_I, [_P, _P, _I, _I, _I64, _I64, _P, _I64,
+                                 ctypes.POINTER(_I32), _I, _P]),
+    "gbsv_apply_all_qubits": (_I, [_P, _P, _I, _I, _I64, _I64, _P, _I64,
+                                   _I64, _P]),
+    "gbsv_apply_phase": (_I, [_P, _I, _P, _I, _P, _I, _BC, _P]),
+    "gbsv_operator_grad_scratch_bytes": (_SZ, [_I64, _I, _I, _I]),
+    "gbsv_operator_grad": (_I, [_P, _P, _I, _I, _I64, _I64,
+                                ctypes.POINTER(_I32), _I, _P, _I, _P, _SZ,
+                                _P]),
+    "gbsv_reduce_scratch_bytes": (_SZ, [_I64, _I64]),
+    "gbsv_norm_squared": (_I, [_P, _I, _I64, _I64, _P, _I, _P, _SZ, _P]),
+    "gbsv_abs_squared": (_I, [_P, _I, _I64, _P, _P]),
+    "gbsv_inner_product": (_I, [_P, _P, _I, _BC, _I64, _I64, _I64, _P, _I,
+                                _P, _SZ, _P]),
+    "gbsv_diag_expectation": (_I, [_P, _I, _P, _I, _BC, _I64, _I64, _I64,
+                                   _P, _I, _P, _SZ, _P]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load(path=None):
+    """Load (once) and return the ctypes handle of libgbsv.so."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    with _lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = path or build_lib.lib_path()
+        if not p.exists():
+            raise RuntimeError(
+                f"libgbsv.so is not built ({p}); run "
+                "`python -c 'import __graft_entry__ as g; g.build()'` or "
+                "`python -m qcware_unitair_gb300.build_lib`.  The engine has "
+                "no CPU fallback.")
+        L = ctypes.CDLL(str(p))
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        if path is None:
+            _lib = L
+        return L
+
+
+def check(status: int, what: str) -> None:
+    if status != GBSV_OK:
+        L = load()
+        detail = L.gbsv_last_error().decode(errors="replace")
+        kind = L.gbsv_status_string(status).decode()
+        raise GbsvError(status, what, f"{kind}: {detail}")
+
+
+def launch_count() -> int:
+    return int(load().gbsv_launch_count())
+
+
+def qubit_array(qubits):
+    arr = (_I32 * max(len(qubits), 1))(*[int(q) for q in qubits])
+    return arr

@@ -1,0 +1,441 @@
+// Batched state reductions with FP64 accumulation: norm_squared,
+// inner_product, diag_expectation_value, and the elementwise abs_squared.
+//
+// unitair computes these with torch elementwise temporaries and a sum in the
+// state's own precision (src/unitair/states/innerprod.py:4-65), i.e. fp32
+// accumulation for complex64 states.  Here each row is read once and
+// accumulated in double; the result is rounded once to the output type.
+//
+// Plan: rows are split into `parts` slices so that the grid fills the GPU.
+// With parts == 1 one block owns a row and writes the result directly.
+// Otherwise every block writes an FP64 partial into caller-provided scratch
+// and a second kernel sums the partials of each row in a fixed order, so the
+// result is deterministic (no atomics).
+#include "common.cuh"
+
+namespace gbsv {
+
+constexpr int RED_THREADS = 256;
+
+struct RowArgs {
+  int64_t rows;
+  int64_t dim;
+  int parts;
+  int64_t part_len;  // elements per part
+  int ndim;          // row broadcast dims
+  int64_t shape[GBSV_MAX_DIMS];
+  int64_t sa[GBSV_MAX_DIMS];
+  int64_t sb[GBSV_MAX_DIMS];
+  int64_t ia, ib;    // inner strides (0 or 1)
+};
+
+struct Plan {
+  int parts;
+  int64_t part_len;
+};
+
+static Plan make_plan(int64_t rows, int64_t dim) {
+  Plan p{1, dim};
+  if (rows <= 0 || dim <= 0) return p;
+  const int64_t want_blocks = (int64_t)sm_count() * 4;
+  const int64_t min_len = 8192;
+  if (rows >= want_blocks || dim <= min_len) return p;
+  int64_t parts = (want_blocks + rows - 1) / rows;
+  const int64_t max_parts = (dim + min_len - 1) / min_len;
+  if (parts > max_parts) parts = max_parts;
+  if (parts > 4096) parts = 4096;
+  if (parts <= 1) return p;
+  int64_t len = (dim + parts - 1) / parts;
+  len = (len + 7) & ~int64_t(7);  // keep slices 16-byte aligned for c64
+  parts = (dim + len - 1) / len;
+  p.parts = (int)parts;
+  p.part_len = len;
+  return p;
+}
+
+__device__ __forceinline__ void row_offsets(const RowArgs& a, int64_t row,
+                                            int64_t* oa, int64_t* ob) {
+  int64_t r = row, xa = 0, xb = 0;
+  for (int d = a.ndim - 1; d >= 0; --d) {
+    const int64_t idx = r % a.shape[d];
+    r /= a.shape[d];
+    xa += idx * a.sa[d];
+    xb += idx * a.sb[d];
+  }
+  *oa = xa;
+  *ob = xb;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum of (x, y); result valid in thread 0.
+__device__ __forceinline__ double2 block_sum2(double x, double y) {
+  __shared__ double sx[RED_THREADS / 32], sy[RED_THREADS / 32];
+  x = warp_sum(x);
+  y = warp_sum(y);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sx[w] = x;
+    sy[w] = y;
+  }
+  __syncthreads();
+  double2 r = make_double2(0.0, 0.0);
+  if (w == 0) {
+    x = l < RED_THREADS / 32 ? sx[l] : 0.0;
+    y = l < RED_THREADS / 32 ? sy[l] : 0.0;
+    r.x = warp_sum(x);
+    r.y = warp_sum(y);
+  }
+  return r;
+}
+
+template <typename T> __device__ __forceinline__ void store_out(T* p, double v);
+template <> __device__ __forceinline__ void store_out<float>(float* p, double v) {
+  *p = (float)v;
+}
+template <> __device__ __forceinline__ void store_out<double>(double* p, double v) {
+  *p = v;
+}
+
+// ---- norm squared: contiguous rows ------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(RED_THREADS)
+    norm2_kernel(const Cx<R>* psi, int64_t dim, int parts, int64_t part_len,
+                 void* out, int out_f64, double* partial) {
+  const int64_t row = blockIdx.x / parts;
+  const int part = blockIdx.x % parts;
+  const int64_t lo = (int64_t)part * part_len;
+  int64_t hi = lo + part_len;
+  if (hi > dim) hi = dim;
+  const Cx<R>* p = psi + row * dim;
+  double acc = 0.0;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += RED_THREADS) {
+    const Cx<R> v = __ldcs(p + i);
+    acc = fma((double)v.x, (double)v.x, acc);
+    acc = fma((double)v.y, (double)v.y, acc);
+  }
+  const double2 s = block_sum2(acc, 0.0);
+  if (threadIdx.x == 0) {
+    if (parts == 1) {
+      if (out_f64)
+        store_out(static_cast<double*>(out) + row, s.x);
+      else
+        store_out(static_cast<float*>(out) + row, s.x);
+    } else {
+      partial[blockIdx.x] = s.x;
+    }
+  }
+}
+
+// Sum `parts` partials (real or complex) of each row in index order.
+__global__ void __launch_bounds__(RED_THREADS)
+    finalize_kernel(const double* partial, int parts, int complex_parts,
+                    int64_t rows, void* out, int out_dtype) {
+  const int64_t row = blockIdx.x;
+  if (row >= rows) return;
+  double x = 0.0, y = 0.0;
+  const int w = complex_parts ? 2 : 1;
+  for (int j = threadIdx.x; j < parts; j += RED_THREADS) {
+    x += partial[(row * parts + j) * w];
+    if (complex_parts) y += partial[(row * parts + j) * w + 1];
+  }
+  const double2 s = block_sum2(x, y);
+  if (threadIdx.x == 0) {
+    switch (out_dtype) {
+      case GBSV_F32: static_cast<float*>(out)[row] = (float)s.x; break;
+      case GBSV_F64: static_cast<double*>(out)[row] = s.x; break;
+      case GBSV_C64:
+        static_cast<float2*>(out)[row] = make_float2((float)s.x, (float)s.y);
+        break;
+      default:
+        static_cast<double2*>(out)[row] = s;
+        break;
+    }
+  }
+}
+
+// ---- inner product over broadcast rows --------------------------------
+template <typename R>
+__global__ void __launch_bounds__(RED_THREADS)
+    inner_kernel(const Cx<R>* a, const Cx<R>* b, RowArgs ra, void* out,
+                 int out_dtype, double* partial) {
+  const int64_t row = blockIdx.x / ra.parts;
+  const int part = blockIdx.x % ra.parts;
+  int64_t oa, ob;
+  row_offsets(ra, row, &oa, &ob);
+  const int64_t lo = (int64_t)part * ra.part_len;
+  int64_t hi = lo + ra.part_len;
+  if (hi > ra.dim) hi = ra.dim;
+  double x = 0.0, y = 0.0;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += RED_THREADS) {
+    const Cx<R> u = a[oa + i * ra.ia];
+    const Cx<R> v = b[ob + i * ra.ib];
+    // conj(u) * v
+    x = fma((double)u.x, (double)v.x, x);
+    x = fma((double)u.y, (double)v.y, x);
+    y = fma((double)u.x, (double)v.y, y);
+    y = fma(-(double)u.y, (double)v.x, y);
+  }
+  const double2 s = block_sum2(x, y);
+  if (threadIdx.x == 0) {
+    if (ra.parts == 1) {
+      if (out_dtype == GBSV_C64)
+        static_cast<float2*>(out)[row] = make_float2((float)s.x, (float)s.y);
+      else
+        static_cast<double2*>(out)[row] = s;
+    } else {
+      partial[2 * blockIdx.x] = s.x;
+      partial[2 * blockIdx.x + 1] = s.y;
+    }
+  }
+}
+
+// ---- diagonal expectation over broadcast rows -------------------------
+template <typename RD, typename R>
+__global__ void __launch_bounds__(RED_THREADS)
+    diag_kernel(const RD* d, const Cx<R>* psi, RowArgs ra, void* out,
+                int out_dtype, double* partial) {
+  const int64_t row = blockIdx.x / ra.parts;
+  const int part = blockIdx.x % ra.parts;
+  int64_t oa, ob;
+  row_offsets(ra, row, &oa, &ob);
+  const int64_t lo = (int64_t)part * ra.part_len;
+  int64_t hi = lo + ra.part_len;
+  if (hi > ra.dim) hi = ra.dim;
+  double acc = 0.0;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += RED_THREADS) {
+    const double w = (double)d[oa + i * ra.ia];
+    const Cx<R> v = psi[ob + i * ra.ib];
+    const double p = fma((double)v.x, (double)v.x, (double)v.y * (double)v.y);
+    acc = fma(w, p, acc);
+  }
+  const double2 s = block_sum2(acc, 0.0);
+  if (threadIdx.x == 0) {
+    if (ra.parts == 1) {
+      if (out_dtype == GBSV_F32)
+        static_cast<float*>(out)[row] = (float)s.x;
+      else
+        static_cast<double*>(out)[row] = s.x;
+    } else {
+      partial[blockIdx.x] = s.x;
+    }
+  }
+}
+
+// ---- abs squared (elementwise) ----------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(256)
+    abs2_kernel(const Cx<R>* psi, R* out, uint64_t count) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const Cx<R> v = __ldcs(psi + i);
+    __stcs(out + i, v.x * v.x + v.y * v.y);
+  }
+}
+
+static int fill_rows(RowArgs* ra, const gbsv_bcast_t* bc, int64_t dim,
+                     int64_t ia, int64_t ib) {
+  if (!bc || bc->ndim < 0 || bc->ndim > GBSV_MAX_DIMS)
+    return set_error(GBSV_ERR_INVALID_ARG, "bad broadcast descriptor");
+  if (dim < 0 || ia < 0 || ia > 1 || ib < 0 || ib > 1)
+    return set_error(GBSV_ERR_INVALID_ARG, "bad inner dimension or stride");
+  ra->ndim = bc->ndim;
+  int64_t rows = 1;
+  for (int d = 0; d < bc->ndim; ++d) {
+    if (bc->shape[d] < 0)
+      return set_error(GBSV_ERR_INVALID_ARG, "negative extent");
+    ra->shape[d] = bc->shape[d];
+    ra->sa[d] = bc->stride_a[d];
+    ra->sb[d] = bc->stride_b[d];
+    rows *= bc->shape[d];
+  }
+  ra->rows = rows;
+  ra->dim = dim;
+  ra->ia = ia;
+  ra->ib = ib;
+  return GBSV_OK;
+}
+
+static int check_scratch(const Plan& p, int64_t rows, int complex_parts,
+                         void* scratch, size_t bytes) {
+  if (p.parts == 1) return GBSV_OK;
+  const size_t need = (size_t)rows * p.parts * sizeof(double) *
+                      (complex_parts ? 2 : 1);
+  if (!scratch || bytes < need)
+    return set_error(GBSV_ERR_SCRATCH,
+                     "reduction needs %zu scratch bytes, got %zu", need,
+                     scratch ? bytes : (size_t)0);
+  if ((uintptr_t)scratch % 16)
+    return set_error(GBSV_ERR_SCRATCH, "scratch must be 16-byte aligned");
+  return GBSV_OK;
+}
+
+static int finalize(const Plan& p, double* partial, int complex_parts,
+                    int64_t rows, void* out, int out_dtype, cudaStream_t st) {
+  if (p.parts == 1) return GBSV_OK;
+  finalize_kernel<<<(unsigned)rows, RED_THREADS, 0, st>>>(
+      partial, p.parts, complex_parts, rows, out, out_dtype);
+  return after_launch("finalize_kernel");
+}
+
+static int check_grid(const Plan& p, int64_t rows) {
+  if ((uint64_t)rows * (uint64_t)p.parts > 0x7fffffffull)
+    return set_error(GBSV_ERR_UNSUPPORTED, "too many rows (%lld)",
+                     (long long)rows);
+  return GBSV_OK;
+}
+
+}  // namespace gbsv
+
+using namespace gbsv;
+
+extern "C" size_t gbsv_reduce_scratch_bytes(int64_t num_rows, int64_t dim) {
+  const Plan p = make_plan(num_rows, dim);
+  if (p.parts == 1) return 0;
+  return (size_t)num_rows * p.parts * 2 * sizeof(double);
+}
+
+extern "C" int gbsv_norm_squared(const void* state, int dtype,
+                                 int64_t num_rows, int64_t dim, void* out,
+                                 int out_dtype, void* scratch,
+                                 size_t scratch_bytes, void* stream) {
+  if (dtype != GBSV_C64 && dtype != GBSV_C128)
+    return set_error(GBSV_ERR_INVALID_ARG, "state must be complex");
+  if (out_dtype != GBSV_F32 && out_dtype != GBSV_F64)
+    return set_error(GBSV_ERR_INVALID_ARG, "output must be float32/float64");
+  if (num_rows < 0 || dim < 0)
+    return set_error(GBSV_ERR_INVALID_ARG, "negative size");
+  if (num_rows == 0) return GBSV_OK;
+  if (!out || (dim > 0 && !state))
+    return set_error(GBSV_ERR_INVALID_ARG, "null pointer");
+  const Plan p = make_plan(num_rows, dim);
+  int rc = check_scratch(p, num_rows, 0, scratch, scratch_bytes);
+  if (!rc) rc = check_grid(p, num_rows);
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const unsigned blocks = (unsigned)(num_rows * p.parts);
+  double* partial = static_cast<double*>(scratch);
+  if (dtype == GBSV_C64)
+    norm2_kernel<float><<<blocks, RED_THREADS, 0, st>>>(
+        static_cast<const float2*>(state), dim, p.parts, p.part_len, out,
+        out_dtype == GBSV_F64, partial);
+  else
+    norm2_kernel<double><<<blocks, RED_THREADS, 0, st>>>(
+        static_cast<const double2*>(state), dim, p.parts, p.part_len, out,
+        out_dtype == GBSV_F64, partial);
+  rc = after_launch("norm2_kernel");
+  if (rc) return rc;
+  return finalize(p, partial, 0, num_rows, out, out_dtype, st);
+}
+
+extern "C" int gbsv_abs_squared(const void* state, int dtype, int64_t count,
+                                void* out, void* stream) {
+  if (dtype != GBSV_C64 && dtype != GBSV_C128)
+    return set_error(GBSV_ERR_INVALID_ARG, "state must be complex");
+  if (count < 0) return set_error(GBSV_ERR_INVALID_ARG, "negative size");
+  if (count == 0) return GBSV_OK;
+  if (!state || !out) return set_error(GBSV_ERR_INVALID_ARG, "null pointer");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  uint64_t blocks = ((uint64_t)count + 255) / 256;
+  const uint64_t cap = (uint64_t)sm_count() * 32;
+  if (blocks > cap) blocks = cap;
+  if (dtype == GBSV_C64)
+    abs2_kernel<float><<<(unsigned)blocks, 256, 0, st>>>(
+        static_cast<const float2*>(state), static_cast<float*>(out), count);
+  else
+    abs2_kernel<double><<<(unsigned)blocks, 256, 0, st>>>(
+        static_cast<const double2*>(state), static_cast<double*>(out), count);
+  return after_launch("abs2_kernel");
+}
+
+extern "C" int gbsv_inner_product(const void* a, const void* b, int dtype,
+                                  const gbsv_bcast_t* bc, int64_t dim,
+                                  int64_t inner_stride_a,
+                                  int64_t inner_stride_b, void* out,
+                                  int out_dtype, void* scratch,
+                                  size_t scratch_bytes, void* stream) {
+  if (dtype != GBSV_C64 && dtype != GBSV_C128)
+    return set_error(GBSV_ERR_INVALID_ARG, "states must be complex");
+  if (out_dtype != GBSV_C64 && out_dtype != GBSV_C128)
+    return set_error(GBSV_ERR_INVALID_ARG, "output must be complex");
+  RowArgs ra{};
+  int rc = fill_rows(&ra, bc, dim, inner_stride_a, inner_stride_b);
+  if (rc) return rc;
+  if (ra.rows == 0) return GBSV_OK;
+  if (!out || (dim > 0 && (!a || !b)))
+    return set_error(GBSV_ERR_INVALID_ARG, "null pointer");
+  const Plan p = make_plan(ra.rows, dim);
+  ra.parts = p.parts;
+  ra.part_len = p.part_len;
+  rc = check_scratch(p, ra.rows, 1, scratch, scratch_bytes);
+  if (!rc) rc = check_grid(p, ra.rows);
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const unsigned blocks = (unsigned)(ra.rows * p.parts);
+  double* partial = static_cast<double*>(scratch);
+  if (dtype == GBSV_C64)
+    inner_kernel<float><<<blocks, RED_THREADS, 0, st>>>(
+        static_cast<const float2*>(a), static_cast<const float2*>(b), ra, out,
+        out_dtype, partial);
+  else
+    inner_kernel<double><<<blocks, RED_THREADS, 0, st>>>(
+        static_cast<const double2*>(a), static_cast<const double2*>(b), ra,
+        out, out_dtype, partial);
+  rc = after_launch("inner_kernel");
+  if (rc) return rc;
+  return finalize(p, partial, 1, ra.rows, out, out_dtype, st);
+}
+
+extern "C" int gbsv_diag_expectation(const void* diag, int diag_dtype,
+                                     const void* state, int state_dtype,
+                                     const gbsv_bcast_t* bc, int64_t dim,
+                                     int64_t inner_stride_diag,
+                                     int64_t inner_stride_state, void* out,
+                                     int out_dtype, void* scratch,
+                                     size_t scratch_bytes, void* stream) {
+  if (state_dtype != GBSV_C64 && state_dtype != GBSV_C128)
+    return set_error(GBSV_ERR_INVALID_ARG, "state must be complex");
+  if (diag_dtype != GBSV_F32 && diag_dtype != GBSV_F64)
+    return set_error(GBSV_ERR_INVALID_ARG, "diagonal must be float32/float64");
+  if (out_dtype != GBSV_F32 && out_dtype != GBSV_F64)
+    return set_error(GBSV_ERR_INVALID_ARG, "output must be float32/float64");
+  RowArgs ra{};
+  int rc = fill_rows(&ra, bc, dim, inner_stride_diag, inner_stride_state);
+  if (rc) return rc;
+  if (ra.rows == 0) return GBSV_OK;
+  if (!out || (dim > 0 && (!diag || !state)))
+    return set_error(GBSV_ERR_INVALID_ARG, "null pointer");
+  const Plan p = make_plan(ra.rows, dim);
+  ra.parts = p.parts;
+  ra.part_len = p.part_len;
+  rc = check_scratch(p, ra.rows, 0, scratch, scratch_bytes);
+  if (!rc) rc = check_grid(p, ra.rows);
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const unsigned blocks = (unsigned)(ra.rows * p.parts);
+  double* partial = static_cast<double*>(scratch);
+  const bool d64 = diag_dtype == GBSV_F64, s64 = state_dtype == GBSV_C128;
+  if (!d64 && !s64)
+    diag_kernel<float, float><<<blocks, RED_THREADS, 0, st>>>(
+        static_cast<const float*>(diag), static_cast<const float2*>(state),
+        ra, out, out_dtype, partial);
+  else if (d64 && !s64)
+    diag_kernel<double, float><<<blocks, RED_THREADS, 0, st>>>(
+        static_cast<const double*>(diag), static_cast<const float2*>(state),
+        ra, out, out_dtype, partial);
+  else if (!d64 && s64)
+    diag_kernel<float, double><<<blocks, RED_THREADS, 0, st>>>(
+        static_cast<const float*>(diag), static_cast<const double2*>(state),
+        ra, out, out_dtype, partial);
+  else
+    diag_kernel<double, double><<<blocks, RED_THREADS, 0, st>>>(
+        static_cast<const double*>(diag), static_cast<const double2*>(state),
+        ra, out, out_dtype, partial);
+  rc = after_launch("diag_kernel");
+  if (rc) return rc;
+  return finalize(p, partial, 0, ra.rows, out, out_dtype, st);
+}

@@ -1,0 +1,386 @@
+"""Mirror of ``unitair.simulation`` on the GB300 kernels.
+
+Same function names, argument meaning, validation order and exception
+types as src/unitair/simulation/operations.py; every gate application is
+one CUDA launch through libgbsv (no permuted copies, no einsum, no CPU path).
+
+Batch rules (operations.py:295-329, checked against the reference):
+  * operator batch == state batch           -> one operator per state
+  * operator unbatched                      -> shared by every state
+  * operator batched, state unbatched       -> the state is broadcast and the
+                                               output takes the operator batch
+  * operator batch broadcasts right-aligned onto the state batch (dims equal
+    or 1)                                   -> operator expanded per state
+  * anything else                           -> RuntimeError
+Documented divergence: unitair silently broadcasts an operator with MORE
+batch dims than a batched state against qubit axes (op (2,3,5) vs state
+(3,5)); here leading operator dims of size 1 are dropped and any other
+extra dim raises RuntimeError.
+"""
+from __future__ import annotations
+
+import math
+from typing import Iterable, Optional, Sequence, Tuple
+
+import torch
+
+from . import _core, _lib
+from .states import (count_qubits, count_qubits_gate_matrix,
+                     StateShapeError)  # noqa: F401  (re-exported errors)
+
+
+# ----------------------------------------------------------------- helpers --
+def _check_dtypes(operator: torch.Tensor, state: torch.Tensor):
+    if operator.dtype != state.dtype:
+        names = {torch.complex64: "ComplexFloat",
+                 torch.complex128: "ComplexDouble",
+                 torch.float32: "Float", torch.float64: "Double"}
+        raise RuntimeError(
+            f"expected scalar type {names.get(state.dtype, state.dtype)} but "
+            f"found {names.get(operator.dtype, operator.dtype)}")
+    _core.complex_code(state.dtype)
+
+
+def _prod(shape) -> int:
+    p = 1
+    for s in shape:
+        p *= int(s)
+    return p
+
+
+class _BatchPlan:
+    """How a (operator, state) pair maps onto the C ABI's two strides."""
+
+    __slots__ = ("out_batch", "num_states", "in_stride", "ops", "op_stride",
+                 "state_expanded", "op_batch_shape")
+
+    def __init__(self, operator, state, n, k):
+        d = 2 ** k
+        N = 2 ** n
+        if operator.dim() < 2:
+            raise RuntimeError(
+                f"Gate with size {operator.size()} is incorrectly shaped for "
+                "an operator batch. Expected size is\n"
+                "  (*optional_batch_dims, 2^k, 2^k)\n"
+                "with k the number of qubits on which the gate acts.")
+        if operator.shape[-2] != d:
+            raise RuntimeError(
+                f"operator of size {tuple(operator.shape)} is not square")
+        state_batch = tuple(state.shape[:-1])
+        op_batch = tuple(operator.shape[:-2])
+        self.op_batch_shape = op_batch
+        self.state_expanded = False
+        if op_batch and not state_batch:
+            self.out_batch = op_batch
+            self.in_stride = 0
+            self.state_expanded = True
+            self.ops = operator.contiguous()
+            self.op_stride = d * d if _prod(op_batch) > 1 else 0
+        else:
+            extra = len(op_batch) - len(state_batch)
+            if extra > 0:
+                if any(s != 1 for s in op_batch[:extra]):
+                    raise RuntimeError(
+                        f"operator batch {op_batch} has more dimensions than "
+                        f"the state batch {state_batch}; unitair would "
+                        "broadcast the extra dimensions against qubit axes. "
+                        "Reshape the operator batch to the state batch.")
+                op_batch = op_batch[extra:]
+                operator = operator.reshape(op_batch + (d, d))
+            for o, s in zip(reversed(op_batch), reversed(state_batch)):
+                if o != s and o != 1:
+                    raise RuntimeError(
+                        f"operator batch {tuple(op_batch)} does not broadcast "
+                        f"onto the state batch {state_batch}")
+            self.out_batch = state_batch
+            self.in_stride = N
+            if _prod(op_batch) == 1:
+                self.ops = operator.reshape(d, d).contiguous()
+                self.op_stride = 0
+            elif tuple(op_batch) == state_batch:
+                self.ops = operator.contiguous()
+                self.op_stride = d * d
+            else:
+                self.ops = operator.expand(state_batch + (d, d)).contiguous()
+                self.op_stride = d * d
+        self.num_states = _prod(self.out_batch)
+
+
+def _launch_apply(ops, op_stride, state_c, in_stride, out, n, qubits,
+                  num_states):
+    dev = state_c.device
+    L = _lib.load()
+    rc = L.gbsv_apply_operator(
+        state_c.data_ptr(), out.data_ptr(), _core.complex_code(state_c.dtype),
+        n, num_states, in_stride, ops.data_ptr(), op_stride,
+        _lib.qubit_array(qubits), len(qubits), _core.stream_of(dev))
+    _lib.check(rc, "apply_operator")
+
+
+def _validate_apply(operator, qubits, state):
+    """operations.py:126-138 plus the duplicate check of utils.py:26."""
+    num_qubits = count_qubits(state)
+    qubits = list(qubits)
+    if not set(qubits).issubset(range(num_qubits)):
+        raise ValueError(
+            f"qubits={qubits} is not consistent with state vector with "
+            f"{num_qubits} qubits.")
+    op_num_qubits = count_qubits_gate_matrix(operator)
+    if len(qubits) != op_num_qubits:
+        raise ValueError(
+            f"Cannot apply operator with {op_num_qubits} to the "
+            f"{len(qubits)} qubit sequence {qubits}.")
+    if len(set(qubits)) != len(qubits):
+        raise ValueError(f"qubits={qubits} contains a repeated qubit.")
+    if op_num_qubits > _lib.MAX_DENSE_QUBITS:
+        raise NotImplementedError(
+            f"operators on more than {_lib.MAX_DENSE_QUBITS} qubits are not "
+            "supported by the GB300 engine")
+    _core.require_cuda(operator, state)
+    _check_dtypes(operator, state)
+    return num_qubits, [int(q) for q in qubits], op_num_qubits
+
+
+def _dagger(ops: torch.Tensor) -> torch.Tensor:
+    return ops.conj().transpose(-1, -2).contiguous()
+
+
+class _ApplyOperator(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, operator, state, qubits, n, k):
+        plan = _BatchPlan(operator, state, n, k)
+        state_c = state.contiguous()
+        out = torch.empty(plan.out_batch + (2 ** n,), dtype=state.dtype,
+                          device=state.device)
+        if plan.num_states:
+            _launch_apply(plan.ops, plan.op_stride, state_c, plan.in_stride,
+                          out, n, qubits, plan.num_states)
+        ctx.qubits, ctx.n, ctx.k = qubits, n, k
+        ctx.plan = plan
+        ctx.op_shape = operator.shape
+        ctx.state_shape = state.shape
+        ctx.save_for_backward(state_c)
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        (state_c,) = ctx.saved_tensors
+        plan, n, k, qubits = ctx.plan, ctx.n, ctx.k, ctx.qubits
+        g = g.contiguous()
+        grad_op = grad_state = None
+        if plan.num_states == 0:
+            return (torch.zeros(ctx.op_shape, dtype=g.dtype, device=g.device),
+                    torch.zeros(ctx.state_shape, dtype=g.dtype,
+                                device=g.device), None, None, None)
+        if ctx.needs_input_grad[1]:
+            gs = torch.empty_like(g)
+            _launch_apply(_dagger(plan.ops), plan.op_stride, g, 2 ** n, gs, n,
+                          qubits, plan.num_states)
+            if plan.state_expanded:
+                gs = gs.reshape(-1, 2 ** n).sum(0)
+            grad_state = gs.reshape(ctx.state_shape)
+        if ctx.needs_input_grad[0]:
+            shared = plan.op_stride == 0
+            d = 2 ** k
+            L = _lib.load()
+            nbytes = int(L.gbsv_operator_grad_scratch_bytes(
+                plan.num_states, n, k, int(shared)))
+            scratch = (torch.empty(nbytes, dtype=torch.uint8, device=g.device)
+                       if nbytes else None)
+            gop = torch.empty((1 if shared else plan.num_states, d, d),
+                              dtype=g.dtype, device=g.device)
+            rc = L.gbsv_operator_grad(
+                g.data_ptr(), state_c.data_ptr(),
+                _core.complex_code(g.dtype), n, plan.num_states,
+                plan.in_stride, _lib.qubit_array(qubits), k, gop.data_ptr(),
+                int(shared), scratch.data_ptr() if scratch is not None else
+                None, nbytes, _core.stream_of(g.device))
+            _lib.check(rc, "operator_grad")
+            target = tuple(ctx.op_shape)
+            if shared:
+                grad_op = gop.reshape(target)
+            else:
+                grad_op = gop.reshape(plan.out_batch + (d, d))
+                core = target[len(target) - grad_op.dim():] \
+                    if len(target) > grad_op.dim() else target
+                grad_op = grad_op.sum_to_size(core).reshape(target)
+        return grad_op, grad_state, None, None, None
+
+
+# ------------------------------------------------------------ public API ---
+def apply_operator(operator: torch.Tensor, qubits: Iterable[int],
+                   state: torch.Tensor) -> torch.Tensor:
+    """Apply a (batch of) k-qubit operator(s) to ``qubits`` of ``state``.
+
+    Drop-in for unitair.simulation.apply_operator (operations.py:45-148):
+    operator (*op_batch, 2^k, 2^k), state (*state_batch, 2^n); the first
+    listed qubit is the operator's most significant index bit; qubit 0 is
+    the most significant bit of the amplitude index.  Returns a new
+    contiguous tensor; differentiable with respect to both inputs.
+    """
+    n, qubits, k = _validate_apply(operator, qubits, state)
+    return _ApplyOperator.apply(operator, state, tuple(qubits), n, k)
+
+
+def apply_operator_(operator: torch.Tensor, qubits: Iterable[int],
+                    state: torch.Tensor) -> torch.Tensor:
+    """In-place apply_operator for engine use: overwrites ``state``.
+
+    The operator batch must be empty or equal to the state batch (or
+    broadcast onto it); no autograd.  ``state`` must be contiguous.
+    """
+    n, qubits, k = _validate_apply(operator, qubits, state)
+    if not state.is_contiguous():
+        raise ValueError("apply_operator_ needs a contiguous state")
+    plan = _BatchPlan(operator, state, n, k)
+    if plan.state_expanded:
+        raise ValueError("apply_operator_ cannot broadcast an unbatched "
+                         "state over an operator batch")
+    if plan.num_states:
+        _launch_apply(plan.ops, plan.op_stride, state, 2 ** n, state, n,
+                      qubits, plan.num_states)
+    return state
+
+
+def act_first_qubits(operator: torch.Tensor,
+                     state: torch.Tensor) -> torch.Tensor:
+    """Apply a k-qubit operator to qubits 0..k-1 (operations.py:236-255)."""
+    num_qubits = count_qubits(state)
+    k = count_qubits_gate_matrix(operator)
+    if num_qubits < k:
+        raise ValueError(f"Attempted to apply a {k}-qubit gate to "
+                         f"{num_qubits} qubit(s).")
+    return apply_operator(operator, range(k), state)
+
+
+def _apply_all_qubits_kernel(operator, state, n, each):
+    """One launch per qubit; operator is (*b, 2, 2), or (*b, n, 2, 2) with
+    one matrix per qubit when ``each``."""
+    plan = _BatchPlan(operator if not each else operator[..., 0, :, :],
+                      state, n, 1)
+    if each:
+        if plan.op_stride:
+            ops = operator.expand(plan.out_batch + (n, 2, 2)).contiguous()
+            op_stride = n * 4
+        else:
+            ops = operator.reshape(n, 2, 2).contiguous()
+            op_stride = 0
+        op_qubit_stride = 4
+    else:
+        ops, op_stride, op_qubit_stride = plan.ops, plan.op_stride, 0
+    state_c = state.contiguous()
+    out = torch.empty(plan.out_batch + (2 ** n,), dtype=state.dtype,
+                      device=state.device)
+    if plan.num_states:
+        rc = _lib.load().gbsv_apply_all_qubits(
+            state_c.data_ptr(), out.data_ptr(),
+            _core.complex_code(state.dtype), n, plan.num_states,
+            plan.in_stride, ops.data_ptr(), op_stride, op_qubit_stride,
+            _core.stream_of(state.device))
+        _lib.check(rc, "apply_all_qubits")
+    return out
+
+
+def apply_all_qubits(operator: torch.Tensor,
+                     state: torch.Tensor) -> torch.Tensor:
+    """The same single-qubit operator on every qubit
+    (operations.py:332-413); batch rules as apply_operator."""
+    if count_qubits_gate_matrix(operator) != 1:
+        raise ValueError(
+            "Expected operator on 1 qubit, found a "
+            f"{count_qubits_gate_matrix(operator)} qubit operator.")
+    num_qubits = count_qubits(state)
+    _core.require_cuda(operator, state)
+    _check_dtypes(operator, state)
+    if num_qubits < 1:
+        raise RuntimeError("apply_all_qubits needs a state of at least one "
+                           "qubit")
+    if torch.is_grad_enabled() and (operator.requires_grad
+                                    or state.requires_grad):
+        out = state
+        for q in range(num_qubits):
+            out = apply_operator(operator, [q], out)
+        return out
+    return _apply_all_qubits_kernel(operator, state, num_qubits, False)
+
+
+def apply_each_qubit(operators: torch.Tensor,
+                     state: torch.Tensor) -> torch.Tensor:
+    """Extension of apply_all_qubits: ``operators`` has shape
+    (*op_batch, n, 2, 2) and operators[..., q, :, :] acts on qubit q.
+
+    unitair's apply_all_qubits rejects per-qubit operator batches; this is
+    the batched per-qubit rotation layer (e.g. RX(angles) with angles of
+    shape (*batch, n)).  Batch rules as apply_operator.
+    """
+    num_qubits = count_qubits(state)
+    if operators.dim() < 3 or operators.shape[-3] != num_qubits or \
+            operators.shape[-1] != 2 or operators.shape[-2] != 2:
+        raise ValueError(
+            f"expected operators of shape (*batch, {num_qubits}, 2, 2), got "
+            f"{tuple(operators.shape)}")
+    _core.require_cuda(operators, state)
+    _check_dtypes(operators, state)
+    if torch.is_grad_enabled() and (operators.requires_grad
+                                    or state.requires_grad):
+        out = state
+        for q in range(num_qubits):
+            out = apply_operator(operators[..., q, :, :], [q], out)
+        return out
+    return _apply_all_qubits_kernel(operators, state, num_qubits, True)
+
+
+class _ApplyPhase(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, angles, state):
+        out = _phase_kernel(angles, state)
+        ctx.save_for_backward(angles, state, out)
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        angles, state, out = ctx.saved_tensors
+        ga = gs = None
+        if ctx.needs_input_grad[1]:
+            gs = _phase_kernel(-angles, g.contiguous())
+            gs = gs.to(state.dtype).sum_to_size(state.shape)
+        if ctx.needs_input_grad[0]:
+            # out = exp(-i a) psi  =>  dL/da = Re(i * g * conj(out))
+            ga = (1j * g * out.conj()).real.to(angles.dtype)
+            ga = ga.sum_to_size(angles.shape)
+        return ga, gs
+
+
+def _phase_kernel(angles: torch.Tensor, state: torch.Tensor) -> torch.Tensor:
+    dev = _core.require_cuda(angles, state)
+    scode = _core.complex_code(state.dtype)
+    if angles.is_complex():
+        raise NotImplementedError("apply_phase takes real angles")
+    if not angles.is_floating_point():
+        angles = angles.to(torch.float32)
+    if angles.dtype not in (torch.float32, torch.float64):
+        angles = angles.to(torch.float32)
+    acode = _core.real_code(angles.dtype)
+    out_dtype = torch.complex128 if (angles.dtype == torch.float64 or
+                                     state.dtype == torch.complex128) \
+        else torch.complex64
+    a = angles.contiguous()
+    s = state.contiguous()
+    out_shape = torch.broadcast_shapes(a.shape, s.shape)
+    out = torch.empty(out_shape, dtype=out_dtype, device=dev)
+    if out.numel() == 0:
+        return out
+    desc = _core.bcast_desc(out_shape, _core.broadcast_strides(a, out_shape),
+                            _core.broadcast_strides(s, out_shape))
+    rc = _lib.load().gbsv_apply_phase(
+        a.data_ptr(), acode, s.data_ptr(), scode, out.data_ptr(),
+        _core.complex_code(out_dtype), desc, _core.stream_of(dev))
+    _lib.check(rc, "apply_phase")
+    return out
+
+
+def apply_phase(angles: torch.Tensor, state: torch.Tensor) -> torch.Tensor:
+    """Multiply the k-th amplitude by exp(-i angles_k) with torch
+    broadcasting (operations.py:15-42).  float64 angles on a complex64
+    state give a complex128 result, as in unitair."""
+    return _ApplyPhase.apply(angles, state)

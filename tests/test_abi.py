@@ -1,0 +1,77 @@
+"""The C-ABI library builds, loads without a GPU and exports exactly what
+include/gbsv.h declares; argument errors come back as status codes without
+touching the device."""
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+from qcware_unitair_gb300 import _lib, build_lib
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "gbsv.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gbsv_\w+)\s*\(", text)))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert "gbsv_apply_operator" in names
+    assert "gbsv_norm_squared" in names
+    assert len(names) >= 12
+
+
+def test_library_exports_every_declared_symbol(lib_built):
+    L = ctypes.CDLL(str(lib_built))
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header():
+    assert sorted(_lib.SIGNATURES) == declared_functions()
+
+
+def test_status_codes_without_gpu(lib_built):
+    L = _lib.load()
+    assert L.gbsv_abi_version() == 1
+    assert L.gbsv_status_string(0) == b"ok"
+    q = _lib.qubit_array([0])
+    # bad dtype, bad qubit, repeated qubit: rejected before any CUDA call
+    assert L.gbsv_apply_operator(None, None, 7, 3, 1, 8, None, 0, q, 1,
+                                 None) == _lib.GBSV_ERR_INVALID_ARG
+    q5 = _lib.qubit_array([5])
+    assert L.gbsv_apply_operator(1, 1, _lib.C64, 3, 1, 8, 1, 0, q5, 1,
+                                 None) == _lib.GBSV_ERR_INVALID_ARG
+    assert b"out of range" in L.gbsv_last_error()
+    q11 = _lib.qubit_array([1, 1])
+    assert L.gbsv_apply_operator(1, 1, _lib.C64, 3, 1, 8, 1, 0, q11, 2,
+                                 None) == _lib.GBSV_ERR_INVALID_ARG
+    assert b"repeated" in L.gbsv_last_error()
+    # zero states: nothing to do, nothing launched
+    before = L.gbsv_launch_count()
+    assert L.gbsv_apply_operator(None, None, _lib.C64, 3, 0, 8, None, 0, q,
+                                 1, None) == 0
+    assert L.gbsv_launch_count() == before
+    assert L.gbsv_norm_squared(None, _lib.C64, 1, 8, None, 9, None, 0,
+                               None) == _lib.GBSV_ERR_INVALID_ARG
+
+
+def test_scratch_sizing_is_consistent(lib_built):
+    L = _lib.load()
+    # small rows: one block per row, no scratch
+    assert L.gbsv_reduce_scratch_bytes(64, 4096) == 0
+
+
+def test_engine_refuses_cpu_tensors():
+    """No CPU fallback: a CPU tensor is an error, not a slow path."""
+    import torch
+    import qcware_unitair_gb300 as ug
+    with pytest.raises(RuntimeError, match="CUDA"):
+        ug.apply_operator(torch.eye(2, dtype=torch.complex64), [0],
+                          torch.ones(4, dtype=torch.complex64))
+    with pytest.raises(RuntimeError, match="CUDA"):
+        ug.norm_squared(torch.ones(4, dtype=torch.complex64))
