@@ -36,7 +36,7 @@ sys.path.insert(0, str(REPO))
 METRIC = "30q c64 HBM GB/s & %peak; served circuits/s, p50/p99 vs plain " \
          "per-gate path"
 WORKLOAD = ("{n}-qubit complex64 state from |0...0>, {g} random "
-            "gates from {H,X,Y,Z,S,T,RX,RY,RZ,CNOT,CZ,SWAP}, one kernel per "
+            "gates from {{H,X,Y,Z,S,T,RX,RY,RZ,CNOT,CZ,SWAP}}, one kernel per "
             "gate")
 
 
