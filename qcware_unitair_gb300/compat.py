@@ -1,0 +1,98 @@
+"""Swap the GB300 engine into an installed ``unitair`` package.
+
+    import unitair
+    from qcware_unitair_gb300 import compat
+    compat.install()          # unitair.simulation.apply_operator -> engine
+
+After install(), unitair's module attributes for the hot path point at the
+engine functions, including the module-level names that unitair's own
+wrappers call (e.g. multi_controlled_x calls operations.apply_operator,
+src/unitair/simulation/operations.py:793-805).  uninstall() restores them.
+
+The engine computes on CUDA tensors only.  ``move_cpu_tensors=True``
+installs adapters that copy CPU inputs to ``device``, run the kernels there
+and copy the results back -- the computation still happens on the GPU; it
+exists so that code written for CPU tensors (such as unitair's own tests)
+can drive the engine unchanged.
+"""
+from __future__ import annotations
+
+import functools
+import importlib
+
+import torch
+
+from . import simulation, states
+
+_TARGETS = {
+    "unitair.simulation.operations": {
+        "apply_operator": simulation.apply_operator,
+        "apply_all_qubits": simulation.apply_all_qubits,
+        "apply_phase": simulation.apply_phase,
+        "act_first_qubits": simulation.act_first_qubits,
+    },
+    "unitair.simulation": {
+        "apply_operator": simulation.apply_operator,
+        "apply_all_qubits": simulation.apply_all_qubits,
+        "apply_phase": simulation.apply_phase,
+        "act_first_qubits": simulation.act_first_qubits,
+    },
+    "unitair.states.innerprod": {
+        "inner_product": states.inner_product,
+        "norm_squared": states.norm_squared,
+        "abs_squared": states.abs_squared,
+        "diag_expectation_value": states.diag_expectation_value,
+    },
+    "unitair.states": {
+        "inner_product": states.inner_product,
+        "norm_squared": states.norm_squared,
+        "abs_squared": states.abs_squared,
+        "diag_expectation_value": states.diag_expectation_value,
+    },
+    "unitair": {
+        "inner_product": states.inner_product,
+        "norm_squared": states.norm_squared,
+        "abs_squared": states.abs_squared,
+        "diag_expectation_value": states.diag_expectation_value,
+    },
+}
+
+_saved: dict = {}
+
+
+def _mover(fn, device):
+    @functools.wraps(fn)
+    def wrapper(*args):
+        cpu = any(isinstance(a, torch.Tensor) and not a.is_cuda for a in args)
+        if not cpu:
+            return fn(*args)
+        moved = [a.to(device) if isinstance(a, torch.Tensor) else a
+                 for a in args]
+        out = fn(*moved)
+        return out.to("cpu") if isinstance(out, torch.Tensor) else out
+    return wrapper
+
+
+def install(move_cpu_tensors: bool = False, device="cuda") -> list:
+    """Patch unitair; return the list of replaced 'module.name' entries."""
+    replaced = []
+    for modname, funcs in _TARGETS.items():
+        try:
+            mod = importlib.import_module(modname)
+        except ImportError:
+            continue
+        for name, fn in funcs.items():
+            if not hasattr(mod, name):
+                continue
+            key = (modname, name)
+            if key not in _saved:
+                _saved[key] = getattr(mod, name)
+            setattr(mod, name, _mover(fn, device) if move_cpu_tensors else fn)
+            replaced.append(f"{modname}.{name}")
+    return replaced
+
+
+def uninstall() -> None:
+    for (modname, name), fn in _saved.items():
+        setattr(importlib.import_module(modname), name, fn)
+    _saved.clear()
