@@ -144,6 +144,22 @@ int gbsv_norm_squared(const void* state, int dtype, int64_t num_rows,
                       int64_t dim, void* out, int out_dtype, void* scratch,
                       size_t scratch_bytes, void* stream);
 
+/* gbsv_norm_squared for callers that cannot allocate device memory: a host
+ * program that reaches the library through a thin FFI and holds only
+ * buffers another runtime gave it has no allocator to call, and a
+ * latency-critical loop must avoid cudaMalloc, which can synchronize the
+ * device.  Same inputs and outputs as gbsv_norm_squared; the FP64 partial
+ * sums live in a fixed 64 KiB device array inside the library (held on every
+ * GPU that loads it until exit) instead of caller scratch, and a request
+ * whose partials do not fit is rejected with GBSV_ERR_UNSUPPORTED.  The
+ * first call on a device looks up that array's device address, so make it
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race.  Calls no cudaMalloc/cudaFree.  No counterpart in the
+ * reference (unitair allocates through torch). */
+int gbsv_norm_squared_noalloc(const void* state, int dtype, int64_t num_rows,
+                              int64_t dim, void* out, int out_dtype,
+                              void* stream);
+
 /* |state[i]|^2 elementwise; out is real of the state's precision.
  * Replaces unitair.states.abs_squared (innerprod.py:4-26). */
 int gbsv_abs_squared(const void* state, int dtype, int64_t count, void* out,

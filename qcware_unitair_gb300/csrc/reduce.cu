@@ -11,6 +11,8 @@
 // Otherwise every block writes an FP64 partial into caller-provided scratch
 // and a second kernel sums the partials of each row in a fixed order, so the
 // result is deterministic (no atomics).
+#include <mutex>
+
 #include "common.cuh"
 
 namespace gbsv {
@@ -438,4 +440,102 @@ extern "C" int gbsv_diag_expectation(const void* diag, int diag_dtype,
   rc = after_launch("diag_kernel");
   if (rc) return rc;
   return finalize(p, partial, 0, ra.rows, out, out_dtype, st);
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free norm_squared.
+//
+// Some callers cannot call cudaMalloc: a host program that reaches this
+// library through a thin FFI and only holds buffers another runtime handed
+// it has no device allocator to call, and a latency-critical loop must not
+// call it because cudaMalloc can synchronize the device and stall work
+// queued on other streams.  gbsv_norm_squared_noalloc serves them: it takes
+// the same inputs and outputs as gbsv_norm_squared but keeps its FP64
+// partial sums in the file-scope device array below instead of caller
+// scratch.
+//
+// The array is NOALLOC_SCRATCH_BYTES (64 KiB) and lives on every GPU that
+// loads this library until the process exits.  Requests whose partials
+// would not fit are rejected with GBSV_ERR_UNSUPPORTED.  Every call shares
+// the array and it keeps the last call's contents; nothing in it has to
+// start at zero, because each call writes every partial it later reads.
+// Calls whose kernels overlap on the GPU (for instance on two streams) race
+// on the array.
+namespace gbsv {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = 64 * 1024;
+static __device__ __align__(256) double
+    g_noalloc_partials[NOALLOC_SCRATCH_BYTES / sizeof(double)];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static std::mutex g_noalloc_mutex;
+static double* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of g_noalloc_partials on the current device, looked up
+// once per device (host code may not use the symbol's host-side name as a
+// device pointer).
+static int noalloc_scratch(double** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess)
+    return set_error(GBSV_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+    return set_error(GBSV_ERR_UNSUPPORTED, "device %d beyond %d", dev,
+                     NOALLOC_MAX_DEVICES);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+    if (e != cudaSuccess || !p)
+      return set_error(GBSV_ERR_CUDA, "cudaGetSymbolAddress: %s",
+                       cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return GBSV_OK;
+}
+
+}  // namespace gbsv
+
+extern "C" int gbsv_norm_squared_noalloc(const void* state, int dtype,
+                                         int64_t num_rows, int64_t dim,
+                                         void* out, int out_dtype,
+                                         void* stream) {
+  if (dtype != GBSV_C64 && dtype != GBSV_C128)
+    return set_error(GBSV_ERR_INVALID_ARG, "state must be complex");
+  if (out_dtype != GBSV_F32 && out_dtype != GBSV_F64)
+    return set_error(GBSV_ERR_INVALID_ARG, "output must be float32/float64");
+  if (num_rows < 0 || dim < 0)
+    return set_error(GBSV_ERR_INVALID_ARG, "negative size");
+  if (num_rows == 0) return GBSV_OK;
+  if (!out || (dim > 0 && !state))
+    return set_error(GBSV_ERR_INVALID_ARG, "null pointer");
+  const Plan p = make_plan(num_rows, dim);
+  int rc = check_grid(p, num_rows);
+  if (rc) return rc;
+  double* partial = nullptr;
+  if (p.parts > 1) {
+    const size_t need = (size_t)num_rows * p.parts * sizeof(double);
+    if (need > NOALLOC_SCRATCH_BYTES)
+      return set_error(GBSV_ERR_UNSUPPORTED,
+                       "norm_squared_noalloc: %lld rows of %lld amplitudes "
+                       "need %zu scratch bytes, more than its fixed %zu",
+                       (long long)num_rows, (long long)dim, need,
+                       NOALLOC_SCRATCH_BYTES);
+    rc = noalloc_scratch(&partial);
+    if (rc) return rc;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const unsigned blocks = (unsigned)(num_rows * p.parts);
+  if (dtype == GBSV_C64)
+    norm2_kernel<float><<<blocks, RED_THREADS, 0, st>>>(
+        static_cast<const float2*>(state), dim, p.parts, p.part_len, out,
+        out_dtype == GBSV_F64, partial);
+  else
+    norm2_kernel<double><<<blocks, RED_THREADS, 0, st>>>(
+        static_cast<const double2*>(state), dim, p.parts, p.part_len, out,
+        out_dtype == GBSV_F64, partial);
+  rc = after_launch("norm2_kernel");
+  if (rc) return rc;
+  return finalize(p, partial, 0, num_rows, out, out_dtype, st);
 }
