@@ -261,6 +261,39 @@ def run_gpu(args, ws, rank, local):
     total_bytes = bytes_per_gate * G * args.steps * ws
     value = total_bytes / (ms / 1e3) / 1e9
 
+    # ---- fused-stage path on the same circuit --------------------------
+    from qcware_unitair_gb300.fusion import Circuit
+    circ = Circuit.from_gates(n, gates)
+    prog = circ.compile(torch.complex64, dev)
+    fused_events = []
+
+    def fused_step(record=None):
+        psi.zero_()
+        psi[0] = 1
+        if record is None:
+            prog.run(psi, inplace=True)
+            return
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        prog.run(psi, inplace=True)
+        e1.record(stream)
+        record.append((e0, e1))
+
+    for _ in range(args.warmup):
+        fused_step()
+    torch.cuda.synchronize()
+    barrier()
+    l1 = _lib.launch_count()
+    for _ in range(args.steps):
+        fused_step(fused_events)
+    torch.cuda.synchronize()
+    fused_launches = _lib.launch_count() - l1
+    fused_ms = statistics.mean(a.elapsed_time(b) for a, b in fused_events)
+    fused_ms = max_over_ranks(fused_ms, dev)
+    fused_norm = float(torch.linalg.vector_norm(psi.to(torch.complex128)))
+    stage_ms = fused_ms / prog.num_passes
+
     # ---- e2e through the public functional API, host buffers -----------
     host_in = torch.zeros(N, dtype=torch.complex64, pin_memory=True)
     host_in[0] = 1
@@ -325,6 +358,21 @@ def run_gpu(args, ws, rank, local):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "api": "qcware_unitair_gb300.apply_operator (functional)",
                 "final_norm_drift": drift},
+        "fused": {
+            "ms_per_step": round(fused_ms, 3), "passes": prog.num_passes,
+            "gates_per_pass": round(G / prog.num_passes, 2),
+            "pass_reduction": round(G / prog.num_passes, 2),
+            "speedup_vs_plain": round((ms / args.steps) / fused_ms, 3),
+            "tile_qubits": prog.m,
+            "hbm_GBs": round(bytes_per_gate * prog.num_passes /
+                             (fused_ms / 1e3) / 1e9, 1),
+            "hbm_frac": round(bytes_per_gate * prog.num_passes /
+                              (fused_ms / 1e3) / 1e9 / peaks()[0], 4),
+            "gate_equivalent_GBs": round(bytes_per_gate * G /
+                                         (fused_ms / 1e3) / 1e9, 1),
+            "stage_ms_mean": round(stage_ms, 4),
+            "launches_per_step": fused_launches // max(1, args.steps),
+            "final_norm": fused_norm},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
     }

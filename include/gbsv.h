@@ -111,6 +111,43 @@ int gbsv_apply_phase(const void* angles, int angle_dtype, const void* state,
                      int state_dtype, void* out, int out_dtype,
                      const gbsv_bcast_t* bc, void* stream);
 
+/* ---- fused gate stages ------------------------------------------------ */
+
+/* One fused-stage gate record (48 bytes, device memory).  kind:
+ *   0 dense 2x2 on tile bit b0;
+ *   1 dense 4x4 on tile bits b0 (matrix MSB) and b1;
+ *   2 diagonal on nq (1 or 2) qubits, each a tile bit (>= 0) or a bit
+ *     outside the tile encoded as -1 - position.
+ * The gate acts only on tiles whose base satisfies (base & cmask) == cval
+ * (controls outside the tile).  Its values sit at pool + mat
+ * (+ state * mat_bstride for per-state gates): 4, 16 or 2^nq complex. */
+typedef struct gbsv_fused_gate {
+  int32_t kind;
+  int32_t nq;
+  int32_t b0, b1;
+  uint64_t cmask, cval;
+  int64_t mat;
+  int64_t mat_bstride;
+} gbsv_fused_gate_t;
+
+/* Largest tile (qubits) a stage may use for this dtype (shared memory). */
+int gbsv_fused_max_tile_qubits(int dtype);
+
+/* Run one fused stage: every tile of 2^tile_qubits amplitudes (tile bits =
+ * tile_positions[0..tile_qubits-1], a HOST array whose first
+ * contiguous_qubits entries are 0..contiguous_qubits-1) is read once from
+ * state_in, the gates are applied in shared memory in order, and the tile
+ * is written once to state_out (in place allowed).  Replaces a run of
+ * unitair apply_operator calls (src/unitair/simulation/operations.py:45-148)
+ * -- each of which makes three passes over the state -- with one pass; the
+ * same idea generalises unitair's host-side single-qubit fusion in
+ * apply_to_qubits (operations.py:416-503, gates/matrix_algebra.py:6-51). */
+int gbsv_run_stage(const void* state_in, void* state_out, int dtype,
+                   int num_qubits, int64_t num_states, int64_t in_stride,
+                   int tile_qubits, int contiguous_qubits,
+                   const int32_t* tile_positions, const void* gates,
+                   int num_gates, const void* pool, void* stream);
+
 /* ---- gradients --------------------------------------------------------- */
 
 /* Scratch bytes gbsv_operator_grad needs (0 = none). */

@@ -1,0 +1,374 @@
+"""Circuits, the fusion planner, and compiled programs.
+
+A ``Circuit`` is an ordered list of gates (matrix + qubits).  ``compile``
+turns it into a ``Program``: a sequence of fused stages (one HBM pass each,
+``gbsv_run_stage``) and, for gates a stage cannot hold, single-gate launches
+(``gbsv_apply_operator``).  ``fuse=False`` gives the plain path: one kernel
+per gate, exactly what a loop of ``apply_operator`` calls launches.
+
+Planner (greedy, in circuit order).  A stage owns m tile bits: the lowest
+``c_min`` amplitude-index bits always (so tiles are made of >= 128-byte
+contiguous runs) plus the bits its gates need.  A gate needs
+  * dense 1-/2-qubit gate: its target bits;
+  * controlled-U (a 4x4 of the form diag(I, U), control = first qubit): the
+    target bit only -- a control outside the tile becomes a per-tile
+    condition;
+  * diagonal gate on 1-2 qubits: nothing -- outside the tile it is a factor
+    per tile, inside a per-amplitude scale.
+A gate joins the current stage if the union of needed bits still fits in m;
+otherwise the stage closes and a new one starts.  Closed stages are topped up
+to m bits with the lowest free positions (longer contiguous runs).
+Wider gates (k >= 3 dense) run as single-gate launches between stages.
+
+This generalises the host-side fusion unitair does in apply_to_qubits
+(src/unitair/simulation/operations.py:416-503, gates/matrix_algebra.py:6-51,
+which only multiplies repeated single-qubit gates on one qubit).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+import torch
+
+from . import _core, _lib
+from .circuits import Gate as NamedGate, gate_matrix
+
+FG_DENSE1, FG_DENSE2, FG_DIAG = 0, 1, 2
+FG_DTYPE = np.dtype([("kind", "<i4"), ("nq", "<i4"), ("b0", "<i4"),
+                     ("b1", "<i4"), ("cmask", "<u8"), ("cval", "<u8"),
+                     ("mat", "<i8"), ("mat_bstride", "<i8")])
+assert FG_DTYPE.itemsize == 48
+
+DENSE, DIAG, CTRL = "dense", "diag", "ctrl"
+
+
+@dataclass
+class CircuitGate:
+    """A gate: ``matrix`` is (d, d) or (B, d, d) (torch tensor, any device)
+    and ``kind`` says which structure the planner may exploit."""
+    matrix: torch.Tensor
+    qubits: Tuple[int, ...]
+    kind: str = DENSE
+
+
+def classify(matrix: torch.Tensor) -> str:
+    """Structure of a host matrix: diagonal, controlled-U (4x4 diag(I, U))
+    or dense.  Exact zeros only (gate builders produce them)."""
+    m = matrix.detach()
+    if m.is_cuda:
+        return DENSE  # no device->host sync just to classify
+    d = m.shape[-1]
+    eye = torch.eye(d, dtype=torch.bool)
+    off = m.masked_select(~eye.expand(m.shape)) if m.numel() else m
+    if not bool((off != 0).any()):
+        return DIAG
+    if d == 4:
+        tl = m[..., :2, :2]
+        if (bool((m[..., :2, 2:] == 0).all()) and
+                bool((m[..., 2:, :2] == 0).all()) and
+                bool((tl == torch.eye(2, dtype=m.dtype)).all())):
+            return CTRL
+    return DENSE
+
+
+class Circuit:
+    """Ordered gates on ``num_qubits`` qubits (qubit 0 = most significant
+    bit of the amplitude index, first listed qubit = matrix MSB)."""
+
+    def __init__(self, num_qubits: int):
+        self.num_qubits = int(num_qubits)
+        self.gates: List[CircuitGate] = []
+
+    def __len__(self):
+        return len(self.gates)
+
+    def append(self, matrix, qubits: Sequence[int],
+               kind: Optional[str] = None) -> "Circuit":
+        if not isinstance(matrix, torch.Tensor):
+            matrix = torch.as_tensor(np.asarray(matrix))
+        qubits = tuple(int(q) for q in qubits)
+        if len(set(qubits)) != len(qubits) or any(
+                q < 0 or q >= self.num_qubits for q in qubits):
+            raise ValueError(f"bad qubits {qubits} for {self.num_qubits} "
+                             "qubits")
+        d = 2 ** len(qubits)
+        if matrix.shape[-2:] != (d, d) or matrix.dim() > 3:
+            raise ValueError(f"matrix {tuple(matrix.shape)} does not fit "
+                             f"{len(qubits)} qubit(s); expected (d, d) or "
+                             "(B, d, d)")
+        self.gates.append(CircuitGate(matrix, qubits,
+                                      kind or classify(matrix)))
+        return self
+
+    # named gates of the canonical set
+    def _named(self, name, qubits, theta=None, kind=DENSE):
+        return self.append(torch.from_numpy(gate_matrix(name, theta)), qubits,
+                           kind)
+
+    def h(self, q): return self._named("H", [q])
+    def x(self, q): return self._named("X", [q])
+    def y(self, q): return self._named("Y", [q])
+    def z(self, q): return self._named("Z", [q], kind=DIAG)
+    def s(self, q): return self._named("S", [q], kind=DIAG)
+    def t(self, q): return self._named("T", [q], kind=DIAG)
+    def cnot(self, c, t): return self._named("CNOT", [c, t], kind=CTRL)
+    def cz(self, a, b): return self._named("CZ", [a, b], kind=DIAG)
+    def swap(self, a, b): return self._named("SWAP", [a, b])
+
+    def rx(self, q, theta): return self._rot("RX", q, theta)
+    def ry(self, q, theta): return self._rot("RY", q, theta)
+    def rz(self, q, theta): return self._rot("RZ", q, theta)
+
+    def _rot(self, name, q, theta):
+        """Rotation by a float or a tensor of per-state angles (B,)."""
+        if isinstance(theta, torch.Tensor) and theta.dim() > 0:
+            from . import gates as G
+            fn = {"RX": G.rx, "RY": G.ry, "RZ": G.rz}[name]
+            m = fn(theta.detach().to(torch.float64).cpu(),
+                   dtype=torch.complex128)
+            return self.append(m, [q], DIAG if name == "RZ" else DENSE)
+        return self._named(name, [q], float(theta),
+                           DIAG if name == "RZ" else DENSE)
+
+    @classmethod
+    def from_gates(cls, num_qubits: int, gates: Sequence[NamedGate]):
+        c = cls(num_qubits)
+        kinds = {"Z": DIAG, "S": DIAG, "T": DIAG, "RZ": DIAG, "CZ": DIAG,
+                 "CNOT": CTRL}
+        for g in gates:
+            c._named(g.name, list(g.qubits), g.theta, kinds.get(g.name, DENSE))
+        return c
+
+    def inverse(self) -> "Circuit":
+        c = Circuit(self.num_qubits)
+        for g in reversed(self.gates):
+            c.append(g.matrix.conj().transpose(-1, -2), g.qubits, g.kind)
+        return c
+
+    def compile(self, dtype=torch.complex64, device="cuda", fuse=True,
+                tile_qubits: Optional[int] = None,
+                min_contiguous: Optional[int] = None) -> "Program":
+        return Program(self, dtype, torch.device(device), fuse, tile_qubits,
+                       min_contiguous)
+
+    def run(self, state: torch.Tensor, fuse: bool = True,
+            inplace: bool = False) -> torch.Tensor:
+        prog = self.compile(state.dtype, state.device, fuse)
+        return prog.run(state, inplace=inplace)
+
+
+# ------------------------------------------------------------ planning ----
+@dataclass
+class _Stage:
+    tile: set
+    gates: List[CircuitGate] = field(default_factory=list)
+
+
+def _needs(g: CircuitGate, n: int):
+    pos = [n - 1 - q for q in g.qubits]
+    k = len(pos)
+    if g.kind == DIAG and k <= 2:
+        return set()
+    if g.kind == CTRL and k == 2:
+        return {pos[1]}
+    if k <= 2:
+        return set(pos)
+    return None  # not stage-able
+
+
+def plan(gates: Sequence[CircuitGate], n: int, m: int, c_min: int):
+    """Greedy stage plan: list of ('stage', _Stage) / ('plain', gate)."""
+    ops = []
+    cur: Optional[_Stage] = None
+    low = set(range(min(c_min, m)))
+    for g in gates:
+        need = _needs(g, n)
+        if need is not None and len(low | need) > m:
+            need = None  # cannot fit even a fresh tile: run it on its own
+        if need is None:
+            if cur is not None:
+                ops.append(("stage", cur))
+                cur = None
+            ops.append(("plain", g))
+            continue
+        if cur is None:
+            cur = _Stage(set(low))
+        if len(cur.tile | need) <= m:
+            cur.tile |= need
+            cur.gates.append(g)
+        else:
+            ops.append(("stage", cur))
+            cur = _Stage(set(low) | need, [g])
+    if cur is not None:
+        ops.append(("stage", cur))
+    for kind, st in ops:
+        if kind == "stage":
+            p = 0
+            while len(st.tile) < m:
+                if p not in st.tile:
+                    st.tile.add(p)
+                p += 1
+    return ops
+
+
+class Program:
+    """A compiled circuit for one dtype/device (see module doc)."""
+
+    def __init__(self, circuit: Circuit, dtype, device, fuse=True,
+                 tile_qubits=None, min_contiguous=None):
+        self.n = n = circuit.num_qubits
+        self.dtype = dtype
+        self.device = device
+        self.code = _core.complex_code(dtype)
+        L = _lib.load()
+        mmax = int(L.gbsv_fused_max_tile_qubits(self.code))
+        if tile_qubits is None:
+            tile_qubits = 13 if dtype == torch.complex64 else 12
+        self.m = min(int(tile_qubits), mmax, n)
+        if min_contiguous is None:
+            min_contiguous = 4 if dtype == torch.complex64 else 3
+        self.c_min = min(int(min_contiguous), self.m)
+        self.batch = None  # per-state gate batch size, if any
+        for g in circuit.gates:
+            if g.matrix.dim() == 3:
+                b = g.matrix.shape[0]
+                if self.batch not in (None, b):
+                    raise ValueError("per-state gates must share one batch "
+                                     "size")
+                self.batch = b
+        if fuse:
+            raw = plan(circuit.gates, n, self.m, self.c_min)
+        else:
+            raw = [("plain", g) for g in circuit.gates]
+        self._build(raw)
+
+    # -- packing ---------------------------------------------------------
+    def _build(self, raw):
+        n, dev, dt = self.n, self.device, self.dtype
+        records = []
+        pool_parts = []
+        pool_len = 0
+
+        def add_pool(values: torch.Tensor):
+            """values (nv,) or (B, nv) -> (offset, bstride)."""
+            nonlocal pool_len
+            v = values.to(device=dev, dtype=dt)
+            off = pool_len
+            if v.dim() == 2:
+                pool_parts.append(v.reshape(-1))
+                pool_len += v.numel()
+                return off, v.shape[1]
+            pool_parts.append(v)
+            pool_len += v.numel()
+            return off, 0
+
+        self.ops = []
+        for kind, item in raw:
+            if kind == "plain":
+                g = item
+                mat = g.matrix.to(device=dev, dtype=dt).contiguous()
+                self.ops.append(("plain", mat, g.qubits))
+                continue
+            st: _Stage = item
+            c = 0
+            while c in st.tile:
+                c += 1
+            c = min(c, self.m)
+            order = list(range(c)) + sorted(p for p in st.tile if p >= c)
+            local = {p: i for i, p in enumerate(order)}
+            first = len(records)
+            for g in st.gates:
+                pos = [n - 1 - q for q in g.qubits]
+                mat = g.matrix
+                rec = np.zeros((), dtype=FG_DTYPE)
+                if g.kind == DIAG:
+                    vals = torch.diagonal(mat, dim1=-2, dim2=-1)
+                    bs = [local[p] if p in local else -1 - p for p in pos]
+                    rec["kind"], rec["nq"] = FG_DIAG, len(pos)
+                    rec["b0"] = bs[0]
+                    rec["b1"] = bs[1] if len(bs) > 1 else 0
+                elif g.kind == CTRL and pos[0] not in local:
+                    vals = mat[..., 2:, 2:].reshape(mat.shape[:-2] + (4,))
+                    rec["kind"], rec["b0"] = FG_DENSE1, local[pos[1]]
+                    rec["cmask"] = rec["cval"] = np.uint64(1 << pos[0])
+                elif len(pos) == 1:
+                    vals = mat.reshape(mat.shape[:-2] + (4,))
+                    rec["kind"], rec["b0"] = FG_DENSE1, local[pos[0]]
+                else:
+                    vals = mat.reshape(mat.shape[:-2] + (16,))
+                    rec["kind"] = FG_DENSE2
+                    rec["b0"], rec["b1"] = local[pos[0]], local[pos[1]]
+                off, bstride = add_pool(vals)
+                rec["mat"], rec["mat_bstride"] = off, bstride
+                records.append(rec)
+            positions = (ctypes.c_int32 * self.m)(*order)
+            self.ops.append(("stage", c, positions, first, len(st.gates)))
+        if records:
+            arr = np.stack(records)
+            self.gate_records = torch.from_numpy(
+                arr.view(np.uint8).copy()).to(dev)
+        else:
+            self.gate_records = torch.empty(0, dtype=torch.uint8, device=dev)
+        self.pool = torch.cat(pool_parts) if pool_parts else torch.zeros(
+            1, dtype=dt, device=dev)
+        self.num_stages = sum(1 for o in self.ops if o[0] == "stage")
+        self.num_plain = sum(1 for o in self.ops if o[0] == "plain")
+
+    @property
+    def num_passes(self) -> int:
+        """HBM passes over the state (one per stage or single-gate launch)."""
+        return len(self.ops)
+
+    # -- running ---------------------------------------------------------
+    def run(self, state: torch.Tensor, inplace: bool = False) -> torch.Tensor:
+        """Apply the program to ``state`` (*batch, 2^n); a per-state gate
+        batch must equal the flattened state batch."""
+        _core.require_cuda(state)
+        if state.dtype != self.dtype:
+            raise RuntimeError(f"program compiled for {self.dtype}, state is "
+                               f"{state.dtype}")
+        if state.shape[-1] != 2 ** self.n:
+            raise ValueError(f"state has {state.shape[-1]} amplitudes, "
+                             f"program is for {self.n} qubits")
+        B = state.numel() >> self.n
+        if self.batch is not None and self.batch != B:
+            raise ValueError(f"per-state gates have batch {self.batch}, "
+                             f"state batch is {B}")
+        if inplace:
+            if not state.is_contiguous():
+                raise ValueError("in-place run needs a contiguous state")
+            out = state
+        else:
+            out = torch.empty_like(state, memory_format=torch.contiguous_format)
+        src = state.contiguous()
+        if B == 0:
+            return out
+        L = _lib.load()
+        stream = _core.stream_of(state.device)
+        N = 2 ** self.n
+        cur = src
+        gp = self.gate_records.data_ptr()
+        pool = self.pool.data_ptr()
+        if not self.ops and cur is not out:
+            out.copy_(cur)
+        for op in self.ops:
+            if op[0] == "stage":
+                _, c, positions, first, count = op
+                rc = L.gbsv_run_stage(cur.data_ptr(), out.data_ptr(),
+                                      self.code, self.n, B, N, self.m, c,
+                                      positions, gp + first * 48, count,
+                                      pool, stream)
+                _lib.check(rc, "run_stage")
+            else:
+                _, mat, qubits = op
+                op_stride = 0 if mat.dim() == 2 else mat.shape[-1] ** 2
+                rc = L.gbsv_apply_operator(
+                    cur.data_ptr(), out.data_ptr(), self.code, self.n, B, N,
+                    mat.data_ptr(), op_stride, _lib.qubit_array(qubits),
+                    len(qubits), stream)
+                _lib.check(rc, "apply_operator")
+            cur = out
+        return out
