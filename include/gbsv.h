@@ -148,6 +148,32 @@ int gbsv_run_stage(const void* state_in, void* state_out, int dtype,
                    const int32_t* tile_positions, const void* gates,
                    int num_gates, const void* pool, void* stream);
 
+/* Register bits per thread of gbsv_run_stage_layouts for this dtype. */
+int gbsv_fused_register_bits(int dtype);
+
+/* One register layout of a stage (32 bytes, device memory): the tile bits
+ * rb[0..R-1] index a thread's R = gbsv_fused_register_bits registers, and
+ * gates[first_gate .. first_gate+num_gates) run in that layout.  In gate
+ * records of a layout stage, dense targets (kind 0, 1) are REGISTER bits;
+ * kind 3 is a 2x2 on register bit b0 applied where tile bit b1 is 1. */
+typedef struct gbsv_layout {
+  int32_t rb[5];
+  int32_t first_gate;
+  int32_t num_gates;
+  int32_t pad_;
+} gbsv_layout_t;
+
+/* gbsv_run_stage with register blocking: the tile is staged in shared
+ * memory, but each layout moves it into registers once and applies all of
+ * its gates there (2^(tile_qubits - R) threads per tile, at most 512). */
+int gbsv_run_stage_layouts(const void* state_in, void* state_out, int dtype,
+                           int num_qubits, int64_t num_states,
+                           int64_t in_stride, int tile_qubits,
+                           int contiguous_qubits,
+                           const int32_t* tile_positions, const void* gates,
+                           const void* layouts, int num_layouts,
+                           const void* pool, void* stream);
+
 /* ---- gradients --------------------------------------------------------- */
 
 /* Scratch bytes gbsv_operator_grad needs (0 = none). */

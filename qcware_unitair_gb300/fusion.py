@@ -150,9 +150,10 @@ class Circuit:
 
     def compile(self, dtype=torch.complex64, device="cuda", fuse=True,
                 tile_qubits: Optional[int] = None,
-                min_contiguous: Optional[int] = None) -> "Program":
+                min_contiguous: Optional[int] = None,
+                layouts: bool = True) -> "Program":
         return Program(self, dtype, torch.device(device), fuse, tile_qubits,
-                       min_contiguous)
+                       min_contiguous, layouts)
 
     def run(self, state: torch.Tensor, fuse: bool = True,
             inplace: bool = False) -> torch.Tensor:
@@ -214,23 +215,200 @@ def plan(gates: Sequence[CircuitGate], n: int, m: int, c_min: int):
     return ops
 
 
+LAYOUT_DTYPE = np.dtype([("rb", "<i4", (5,)), ("first_gate", "<i4"),
+                         ("num_gates", "<i4"), ("pad", "<i4")])
+assert LAYOUT_DTYPE.itemsize == 32
+FG_CDENSE1, FG_REAL1, FG_ANTI1, FG_CANTI1, FG_PERM2, FG_RDIAG = 3, 4, 5, 6, 7, 8
+
+
+def _host(m: torch.Tensor) -> Optional[torch.Tensor]:
+    """The matrix on the host, or None when looking would need a sync."""
+    return None if m.is_cuda else m.detach()
+
+
+def _is_real(m) -> bool:
+    h = _host(m)
+    if h is None:
+        return False
+    return (not h.is_complex()) or bool((h.imag == 0).all())
+
+
+def _is_anti(m) -> bool:
+    h = _host(m)
+    return h is not None and bool((h[..., 0, 0] == 0).all()) and bool(
+        (h[..., 1, 1] == 0).all())
+
+
+def _is_unit_swap(m) -> bool:
+    h = _host(m)
+    return h is not None and bool((h[..., 0, 1] == 1).all()) and bool(
+        (h[..., 1, 0] == 1).all())
+
+
+def _perm_code(m) -> Optional[int]:
+    """4x4 0/1 permutation shared by every batch entry -> packed sources."""
+    h = _host(m)
+    if h is None:
+        return None
+    h = h.reshape(-1, 4, 4)
+    if not bool(((h == 0) | (h == 1)).all()):
+        return None
+    code = 0
+    for r in range(4):
+        cols = [c for c in range(4) if bool((h[:, r, c] == 1).all())]
+        if len(cols) != 1 or bool((h[:, r, :] != 0).sum(-1).ne(1).any()):
+            return None
+        code |= cols[0] << (2 * r)
+    return code
+
+
+def _dense1_kind(u) -> Tuple[int, int]:
+    """(kind, nq flag) for a 2x2 applied on a register bit."""
+    if _is_anti(u):
+        return FG_ANTI1, int(_is_unit_swap(u))
+    if _is_real(u):
+        return FG_REAL1, 0
+    return FG_DENSE1, 0
+
+
+def _record(g: CircuitGate, n: int, local: dict, kreg: Optional[dict],
+            rb: int = 0):
+    """Gate record and its pool values.  ``local`` maps positions to tile
+    bits; ``kreg`` (register-blocked stages) maps tile bits to register
+    bits, None for the shared-memory stage kernel."""
+    pos = [n - 1 - q for q in g.qubits]
+    mat = g.matrix
+    rec = np.zeros((), dtype=FG_DTYPE)
+    reg = (lambda b: kreg[b]) if kreg is not None else (lambda b: b)
+    if kreg is not None:
+        return _layout_record(g, pos, mat, rec, local, kreg, rb)
+    if g.kind == DIAG:
+        vals = torch.diagonal(mat, dim1=-2, dim2=-1)
+        bs = [local[p] if p in local else -1 - p for p in pos]
+        rec["kind"], rec["nq"] = FG_DIAG, len(pos)
+        rec["b0"] = bs[0]
+        rec["b1"] = bs[1] if len(bs) > 1 else 0
+    elif g.kind == CTRL and pos[0] not in local:
+        vals = mat[..., 2:, 2:].reshape(mat.shape[:-2] + (4,))
+        rec["kind"], rec["b0"] = FG_DENSE1, reg(local[pos[1]])
+        rec["cmask"] = rec["cval"] = np.uint64(1 << pos[0])
+    elif (g.kind == CTRL and kreg is not None
+          and local[pos[0]] not in kreg):
+        # control on a thread bit: a per-thread condition
+        vals = mat[..., 2:, 2:].reshape(mat.shape[:-2] + (4,))
+        rec["kind"] = FG_CDENSE1
+        rec["b0"], rec["b1"] = reg(local[pos[1]]), local[pos[0]]
+    elif len(pos) == 1:
+        vals = mat.reshape(mat.shape[:-2] + (4,))
+        rec["kind"], rec["b0"] = FG_DENSE1, reg(local[pos[0]])
+    else:
+        vals = mat.reshape(mat.shape[:-2] + (16,))
+        rec["kind"] = FG_DENSE2
+        rec["b0"], rec["b1"] = reg(local[pos[0]]), reg(local[pos[1]])
+    return rec, vals
+
+
+def _layout_record(g, pos, mat, rec, local, kreg, rb):
+    """Record for a register-blocked stage, specialised by structure."""
+    if g.kind == DIAG:
+        vals = torch.diagonal(mat, dim1=-2, dim2=-1)
+        enc = []
+        for p in pos:
+            if p not in local:
+                enc.append(-1 - p)
+            elif local[p] in kreg:
+                enc.append(kreg[local[p]])
+            else:
+                enc.append(rb + local[p])
+        rec["kind"], rec["nq"] = FG_RDIAG, len(pos)
+        rec["b0"] = enc[0]
+        rec["b1"] = enc[1] if len(enc) > 1 else 0
+        return rec, vals
+    if g.kind == CTRL:
+        u = mat[..., 2:, 2:]
+        vals4 = u.reshape(mat.shape[:-2] + (4,))
+        c, t = local.get(pos[0]), local[pos[1]]
+        if c is None:  # control outside the tile: a per-tile condition
+            kind, flag = _dense1_kind(u)
+            rec["kind"], rec["nq"], rec["b0"] = kind, flag, kreg[t]
+            rec["cmask"] = rec["cval"] = np.uint64(1 << pos[0])
+            return rec, vals4
+        if c not in kreg:  # control on a thread bit
+            if _is_anti(u):
+                rec["kind"], rec["nq"] = FG_CANTI1, int(_is_unit_swap(u))
+            else:
+                rec["kind"] = FG_CDENSE1
+            rec["b0"], rec["b1"] = kreg[t], c
+            return rec, vals4
+    if len(pos) == 1:
+        kind, flag = _dense1_kind(mat)
+        rec["kind"], rec["nq"], rec["b0"] = kind, flag, kreg[local[pos[0]]]
+        return rec, mat.reshape(mat.shape[:-2] + (4,))
+    code = _perm_code(mat)
+    rec["b0"], rec["b1"] = kreg[local[pos[0]]], kreg[local[pos[1]]]
+    if code is not None:
+        rec["kind"], rec["nq"] = FG_PERM2, code
+    else:
+        rec["kind"] = FG_DENSE2
+    return rec, mat.reshape(mat.shape[:-2] + (16,))
+
+
+def _plan_layouts(gates, n, local, m, rb):
+    """Group a stage's gates into register layouts (rb tile bits each)."""
+    out = []
+    need_all: set = set()
+    cur: list = []
+    for g in gates:
+        pos = [n - 1 - q for q in g.qubits]
+        if g.kind == DIAG:
+            need = set()
+        elif g.kind == CTRL and pos[0] not in local:
+            need = {local[pos[1]]}
+        elif g.kind == CTRL:
+            need = {local[pos[1]]}
+        else:
+            need = {local[p] for p in pos}
+        if len(need_all | need) <= rb:
+            need_all |= need
+            cur.append(g)
+        else:
+            out.append((need_all, cur))
+            need_all, cur = set(need), [g]
+    out.append((need_all, cur))
+    layouts = []
+    for need, lg in out:
+        bits = sorted(need)
+        b = m - 1  # top up with high tile bits: low bits stay thread bits
+        while len(bits) < rb:
+            if b not in need:
+                bits.append(b)
+            b -= 1
+        layouts.append((bits, lg))
+    return layouts
+
+
 class Program:
     """A compiled circuit for one dtype/device (see module doc)."""
 
     def __init__(self, circuit: Circuit, dtype, device, fuse=True,
-                 tile_qubits=None, min_contiguous=None):
+                 tile_qubits=None, min_contiguous=None, layouts=True):
         self.n = n = circuit.num_qubits
         self.dtype = dtype
         self.device = device
         self.code = _core.complex_code(dtype)
         L = _lib.load()
         mmax = int(L.gbsv_fused_max_tile_qubits(self.code))
+        self.rb = int(L.gbsv_fused_register_bits(self.code))
         if tile_qubits is None:
-            tile_qubits = 13 if dtype == torch.complex64 else 12
+            # 12 tile qubits (32 KiB c64 tiles, 4 CTAs per SM) measured
+            # fastest on the 30-qubit random circuit among m = 12..14
+            tile_qubits = 12
         self.m = min(int(tile_qubits), mmax, n)
         if min_contiguous is None:
             min_contiguous = 4 if dtype == torch.complex64 else 3
         self.c_min = min(int(min_contiguous), self.m)
+        # register-blocked stages need rb <= m and at most 512 threads
+        self.use_layouts = bool(layouts) and self.rb <= self.m <= self.rb + 9
         self.batch = None  # per-state gate batch size, if any
         for g in circuit.gates:
             if g.matrix.dim() == 3:
@@ -249,6 +427,7 @@ class Program:
     def _build(self, raw):
         n, dev, dt = self.n, self.device, self.dtype
         records = []
+        layouts = []
         pool_parts = []
         pool_len = 0
 
@@ -279,32 +458,31 @@ class Program:
             c = min(c, self.m)
             order = list(range(c)) + sorted(p for p in st.tile if p >= c)
             local = {p: i for i, p in enumerate(order)}
+            positions = (ctypes.c_int32 * self.m)(*order)
+            if self.use_layouts:
+                first_layout = len(layouts)
+                for rbits, lgates in _plan_layouts(st.gates, n, local,
+                                                   self.m, self.rb):
+                    first = len(records)
+                    kreg = {b: k for k, b in enumerate(rbits)}
+                    for g in lgates:
+                        rec, vals = _record(g, n, local, kreg, self.rb)
+                        off, bstride = add_pool(vals)
+                        rec["mat"], rec["mat_bstride"] = off, bstride
+                        records.append(rec)
+                    lay = np.zeros((), dtype=LAYOUT_DTYPE)
+                    lay["rb"][:len(rbits)] = rbits
+                    lay["first_gate"], lay["num_gates"] = first, len(lgates)
+                    layouts.append(lay)
+                self.ops.append(("layouts", c, positions, first_layout,
+                                 len(layouts) - first_layout))
+                continue
             first = len(records)
             for g in st.gates:
-                pos = [n - 1 - q for q in g.qubits]
-                mat = g.matrix
-                rec = np.zeros((), dtype=FG_DTYPE)
-                if g.kind == DIAG:
-                    vals = torch.diagonal(mat, dim1=-2, dim2=-1)
-                    bs = [local[p] if p in local else -1 - p for p in pos]
-                    rec["kind"], rec["nq"] = FG_DIAG, len(pos)
-                    rec["b0"] = bs[0]
-                    rec["b1"] = bs[1] if len(bs) > 1 else 0
-                elif g.kind == CTRL and pos[0] not in local:
-                    vals = mat[..., 2:, 2:].reshape(mat.shape[:-2] + (4,))
-                    rec["kind"], rec["b0"] = FG_DENSE1, local[pos[1]]
-                    rec["cmask"] = rec["cval"] = np.uint64(1 << pos[0])
-                elif len(pos) == 1:
-                    vals = mat.reshape(mat.shape[:-2] + (4,))
-                    rec["kind"], rec["b0"] = FG_DENSE1, local[pos[0]]
-                else:
-                    vals = mat.reshape(mat.shape[:-2] + (16,))
-                    rec["kind"] = FG_DENSE2
-                    rec["b0"], rec["b1"] = local[pos[0]], local[pos[1]]
+                rec, vals = _record(g, n, local, None)
                 off, bstride = add_pool(vals)
                 rec["mat"], rec["mat_bstride"] = off, bstride
                 records.append(rec)
-            positions = (ctypes.c_int32 * self.m)(*order)
             self.ops.append(("stage", c, positions, first, len(st.gates)))
         if records:
             arr = np.stack(records)
@@ -312,9 +490,17 @@ class Program:
                 arr.view(np.uint8).copy()).to(dev)
         else:
             self.gate_records = torch.empty(0, dtype=torch.uint8, device=dev)
+        if layouts:
+            arr = np.stack(layouts)
+            self.layout_records = torch.from_numpy(
+                arr.view(np.uint8).copy()).to(dev)
+        else:
+            self.layout_records = torch.empty(0, dtype=torch.uint8,
+                                              device=dev)
+        self.num_layouts = len(layouts)
         self.pool = torch.cat(pool_parts) if pool_parts else torch.zeros(
             1, dtype=dt, device=dev)
-        self.num_stages = sum(1 for o in self.ops if o[0] == "stage")
+        self.num_stages = sum(1 for o in self.ops if o[0] != "plain")
         self.num_plain = sum(1 for o in self.ops if o[0] == "plain")
 
     @property
@@ -351,6 +537,7 @@ class Program:
         N = 2 ** self.n
         cur = src
         gp = self.gate_records.data_ptr()
+        lp = self.layout_records.data_ptr()
         pool = self.pool.data_ptr()
         if not self.ops and cur is not out:
             out.copy_(cur)
@@ -362,6 +549,13 @@ class Program:
                                       positions, gp + first * 48, count,
                                       pool, stream)
                 _lib.check(rc, "run_stage")
+            elif op[0] == "layouts":
+                _, c, positions, first, count = op
+                rc = L.gbsv_run_stage_layouts(
+                    cur.data_ptr(), out.data_ptr(), self.code, self.n, B, N,
+                    self.m, c, positions, gp, lp + first * 32, count, pool,
+                    stream)
+                _lib.check(rc, "run_stage_layouts")
             else:
                 _, mat, qubits = op
                 op_stride = 0 if mat.dim() == 2 else mat.shape[-1] ** 2
