@@ -194,6 +194,45 @@ int gbsv_operator_grad(const void* grad_out, const void* state_in, int dtype,
                        void* grad_ops, int shared, void* scratch,
                        size_t scratch_bytes, void* stream);
 
+/* ---- adjoint differentiation ------------------------------------------ */
+
+/* One term c * P of a Pauli-sum observable (32 bytes, device memory).
+ * P = i^(#Y) X^xmask Z^zmask over amplitude-index bit positions (qubit q is
+ * bit n-1-q; a Y sets the bit in both masks), and (re, im) = c * i^(#Y). */
+typedef struct gbsv_pauli_term {
+  uint64_t xmask, zmask;
+  double re, im;
+} gbsv_pauli_term_t;
+
+/* out = H psi for H = sum_k terms[k] (at most 256 terms; out != psi).
+ * No counterpart in unitair, whose observables are diagonals
+ * (diag_expectation_value, src/unitair/states/innerprod.py:49-59); X/Y
+ * terms such as X_i X_{i+1} need this. */
+int gbsv_pauli_sum_apply(const void* psi, void* out, int dtype,
+                         int num_qubits, int64_t num_states,
+                         const void* terms, int num_terms, void* stream);
+
+/* Scratch bytes gbsv_adjoint_rotation_step needs. */
+size_t gbsv_adjoint_scratch_bytes(int64_t num_states, int num_qubits);
+
+/* One backward step of the adjoint method for a rotation
+ * U = exp(-i theta/2 P) on `qubit` (generator 0 = X, 1 = Y, 2 = Z), with
+ * theta_s = angle_scale * angles[s * angle_stride] (float32 or float64):
+ *   grad[s * grad_stride] += grad_factor * Im <lam_s| P |psi_s>
+ * (FP64 accumulation), then psi_s <- U^dag psi_s and lam_s <- U^dag lam_s
+ * in place.  One read and one write of both states.  Replaces torch
+ * autograd through unitair's gate application
+ * (src/unitair/simulation/operations.py:45-148), which stores every
+ * intermediate state. */
+int gbsv_adjoint_rotation_step(void* psi, void* lam, int dtype,
+                               int num_qubits, int64_t num_states, int qubit,
+                               int generator, const void* angles,
+                               int angle_dtype, int64_t angle_stride,
+                               double angle_scale, double* grad,
+                               int64_t grad_stride, double grad_factor,
+                               void* scratch, size_t scratch_bytes,
+                               void* stream);
+
 /* ---- reductions (FP64 accumulation) ----------------------------------- */
 
 /* Scratch bytes a reduction over num_rows rows of length dim needs; 0 means

@@ -69,6 +69,11 @@ SIGNATURES = {
     "gbsv_operator_grad": (_I, [_P, _P, _I, _I, _I64, _I64,
                                 ctypes.POINTER(_I32), _I, _P, _I, _P, _SZ,
                                 _P]),
+    "gbsv_pauli_sum_apply": (_I, [_P, _P, _I, _I, _I64, _P, _I, _P]),
+    "gbsv_adjoint_scratch_bytes": (_SZ, [_I64, _I]),
+    "gbsv_adjoint_rotation_step": (_I, [_P, _P, _I, _I, _I64, _I, _I, _P, _I,
+                                        _I64, ctypes.c_double, _P, _I64,
+                                        ctypes.c_double, _P, _SZ, _P]),
     "gbsv_reduce_scratch_bytes": (_SZ, [_I64, _I64]),
     "gbsv_norm_squared": (_I, [_P, _I, _I64, _I64, _P, _I, _P, _SZ, _P]),
     "gbsv_norm_squared_noalloc": (_I, [_P, _I, _I64, _I64, _P, _I, _P]),

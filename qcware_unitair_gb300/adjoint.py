@@ -1,0 +1,346 @@
+"""Adjoint differentiation of expectation values of parameterised circuits.
+
+    pc = ParamCircuit(n, num_params)
+    pc.ry(q, p); pc.rz(q, p); pc.cz(a, b); pc.end_layer()
+    H = PauliSum(n).z(0).xx(0, 1, coeff=0.5)
+    values = expectation(pc, params, H)            # (B,) float64, autograd
+    values.mean().backward()                       # adjoint sweep, no tape
+
+Rotations follow unitair's convention (src/unitair/gates/gates.py:6-91):
+RX(theta) = exp_x(theta / 2) = exp(-i theta/2 X), likewise RY, RZ; the angle
+of a rotation is ``scale * params[b, p]`` per batch entry b.
+
+The forward pass runs the circuit as a fused program (one HBM pass per
+stage) and keeps the state at checkpoints every ~sqrt(depth) layers.  The
+backward pass starts from lambda = H psi_L (gbsv_pauli_sum_apply) and walks
+the gates in reverse with gbsv_adjoint_rotation_step (gradient Im<l|P|psi>
+accumulated in FP64, then U^dag applied to psi and lambda in the same pass);
+fixed gates are uncomputed on both states in one launch.  At each
+checkpoint the uncomputed psi is replaced by the stored forward state, so
+rounding drift never accumulates over more than one segment.
+This replaces torch autograd through unitair's apply_operator, which keeps
+every intermediate state (one per gate) alive for the backward pass.
+"""
+from __future__ import annotations
+
+import math
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _core, _lib, states
+from .circuits import gate_matrix
+from .fusion import CTRL, DENSE, DIAG, Circuit
+
+GEN = {"X": 0, "Y": 1, "Z": 2}
+
+
+class PauliSum:
+    """H = sum_k c_k P_k with real c_k and Pauli strings P_k."""
+
+    def __init__(self, num_qubits: int):
+        self.num_qubits = num_qubits
+        self.terms: List[tuple] = []  # (coeff, {qubit: 'X'|'Y'|'Z'})
+
+    def add(self, coeff: float, paulis: Dict[int, str]) -> "PauliSum":
+        for q, p in paulis.items():
+            if p not in "XYZ" or not 0 <= q < self.num_qubits:
+                raise ValueError(f"bad Pauli {p} on qubit {q}")
+        self.terms.append((float(coeff), dict(paulis)))
+        return self
+
+    def z(self, q, coeff=1.0):
+        return self.add(coeff, {q: "Z"})
+
+    def xx(self, a, b, coeff=1.0):
+        return self.add(coeff, {a: "X", b: "X"})
+
+    def term_array(self) -> np.ndarray:
+        """Records matching gbsv_pauli_term_t (xmask, zmask, re, im)."""
+        n = self.num_qubits
+        dt = np.dtype([("x", "<u8"), ("z", "<u8"), ("re", "<f8"),
+                       ("im", "<f8")])
+        out = np.zeros(len(self.terms), dtype=dt)
+        for k, (c, ps) in enumerate(self.terms):
+            xm = zm = 0
+            ny = 0
+            for q, p in ps.items():
+                bit = 1 << (n - 1 - q)
+                if p in "XY":
+                    xm |= bit
+                if p in "ZY":
+                    zm |= bit
+                ny += p == "Y"
+            phase = 1j ** ny
+            out[k] = (xm, zm, c * phase.real, c * phase.imag)
+        return out
+
+    def dense(self) -> np.ndarray:
+        """2^n x 2^n matrix (small n; for tests)."""
+        n = self.num_qubits
+        P = {"I": np.eye(2), "X": np.array([[0, 1], [1, 0]]),
+             "Y": np.array([[0, -1j], [1j, 0]]), "Z": np.diag([1, -1])}
+        H = np.zeros((2 ** n, 2 ** n), dtype=np.complex128)
+        for c, ps in self.terms:
+            m = np.array([[1.0]])
+            for q in range(n):
+                m = np.kron(m, P[ps.get(q, "I")])
+            H += c * m
+        return H
+
+
+def hardware_efficient_ansatz(num_qubits: int, layers: int):
+    """Each layer applies U = RY(theta) RZ(phi) to every qubit (RZ acts
+    first), then a ring of CZ(q, q+1 mod n).  Parameter (layer, qubit, k)
+    has index (layer * n + qubit) * 2 + k, k = 0 for theta and 1 for phi,
+    i.e. a (B, layers, n, 2) tensor reshaped to (B, layers * n * 2)."""
+    n = num_qubits
+    pc = ParamCircuit(n, layers * n * 2)
+    for l in range(layers):
+        for q in range(n):
+            base = (l * n + q) * 2
+            pc.rz(q, base + 1)
+            pc.ry(q, base + 0)
+        for q in range(n):
+            if n > 1 and (q + 1 < n or n > 2):
+                pc.cz(q, (q + 1) % n)
+        pc.end_layer()
+    return pc
+
+
+class ParamCircuit:
+    """Rotations driven by a (B, num_params) parameter tensor plus fixed
+    gates; ``end_layer`` marks layer boundaries for checkpointing."""
+
+    def __init__(self, num_qubits: int, num_params: int):
+        self.num_qubits = num_qubits
+        self.num_params = num_params
+        self.ops: list = []
+        self.layer_ends: List[int] = []
+
+    def _rot(self, gen, q, p, scale):
+        if not 0 <= p < self.num_params:
+            raise ValueError(f"parameter index {p} out of range")
+        if not 0 <= q < self.num_qubits:
+            raise ValueError(f"qubit {q} out of range")
+        self.ops.append(("rot", gen, int(q), int(p), float(scale)))
+        return self
+
+    def rx(self, q, p, scale=1.0): return self._rot("X", q, p, scale)
+    def ry(self, q, p, scale=1.0): return self._rot("Y", q, p, scale)
+    def rz(self, q, p, scale=1.0): return self._rot("Z", q, p, scale)
+
+    def gate(self, matrix, qubits, kind: Optional[str] = None):
+        m = torch.as_tensor(np.asarray(matrix, dtype=np.complex128))
+        self.ops.append(("fixed", m, tuple(int(q) for q in qubits), kind))
+        return self
+
+    def h(self, q): return self.gate(gate_matrix("H"), [q], DENSE)
+    def cz(self, a, b): return self.gate(gate_matrix("CZ"), [a, b], DIAG)
+    def cnot(self, c, t): return self.gate(gate_matrix("CNOT"), [c, t], CTRL)
+
+    def end_layer(self):
+        self.layer_ends.append(len(self.ops))
+        return self
+
+    # -- segments for checkpoints ---------------------------------------
+    def segments(self, every: Optional[int] = None) -> List[tuple]:
+        """Op ranges [a, b) between checkpoints, every ~sqrt(depth)
+        layers (or ~sqrt(ops) without layer marks)."""
+        ends = [e for e in self.layer_ends if 0 < e <= len(self.ops)]
+        if ends and ends[-1] != len(self.ops):
+            ends.append(len(self.ops))
+        if not ends:
+            k = every or max(1, int(math.ceil(math.sqrt(len(self.ops)))))
+            ends = list(range(k, len(self.ops), k)) + [len(self.ops)]
+        else:
+            k = every or max(1, int(math.ceil(math.sqrt(len(ends)))))
+            ends = ends[k - 1::k] if len(ends) > k else []
+            if not ends or ends[-1] != len(self.ops):
+                ends.append(len(self.ops))
+        out, a = [], 0
+        for e in ends:
+            if e > a:
+                out.append((a, e))
+            a = e
+        return out or [(0, 0)]
+
+    # -- building blocks ---------------------------------------------------
+    def _segment_circuit(self, a, b, params, dtype) -> Circuit:
+        """Ops [a, b) as a Circuit with per-state rotation matrices."""
+        c = Circuit(self.num_qubits)
+        B = params.shape[0]
+        for op in self.ops[a:b]:
+            if op[0] == "fixed":
+                _, m, qs, kind = op
+                c.append(m, qs, kind)
+                continue
+            _, gen, q, p, scale = op
+            th = params[:, p].detach().to(torch.float64) * (0.5 * scale)
+            cs, sn = torch.cos(th), torch.sin(th)
+            z = torch.zeros_like(cs)
+            if gen == "X":
+                m = torch.stack([torch.complex(cs, z), torch.complex(z, -sn),
+                                 torch.complex(z, -sn), torch.complex(cs, z)],
+                                -1)
+                kind = DENSE
+            elif gen == "Y":
+                m = torch.stack([torch.complex(cs, z), torch.complex(-sn, z),
+                                 torch.complex(sn, z), torch.complex(cs, z)],
+                                -1)
+                kind = DENSE
+            else:
+                m = torch.stack([torch.complex(cs, -sn), torch.complex(z, z),
+                                 torch.complex(z, z), torch.complex(cs, sn)],
+                                -1)
+                kind = DIAG
+            c.append(m.reshape(B, 2, 2).to(dtype), [q], kind)
+        return c
+
+
+def _initial_state(n, B, dtype, device, psi0):
+    if psi0 is None:
+        s = torch.zeros(B, 2 ** n, dtype=dtype, device=device)
+        s[:, 0] = 1
+        return s
+    s = psi0.to(device=device, dtype=dtype)
+    if s.dim() == 1:
+        s = s.expand(B, -1)
+    return s.reshape(B, 2 ** n).contiguous()
+
+
+def _forward(pc: ParamCircuit, params, dtype, psi0, checkpoints: bool):
+    """Run the circuit; return (psi_L, [psi at each segment start])."""
+    n, B = pc.num_qubits, params.shape[0]
+    dev = params.device
+    psi = _initial_state(n, B, dtype, dev, psi0)
+    saved = []
+    for a, b in pc.segments():
+        if checkpoints:
+            saved.append(psi.clone())
+        if b > a:
+            prog = pc._segment_circuit(a, b, params, dtype).compile(dtype,
+                                                                    dev)
+            prog.run(psi, inplace=True)
+    return psi, saved
+
+
+def _pauli_apply(H: PauliSum, psi: torch.Tensor, out: torch.Tensor):
+    terms = torch.from_numpy(H.term_array().view(np.uint8).copy()).to(
+        psi.device)
+    n = H.num_qubits
+    rc = _lib.load().gbsv_pauli_sum_apply(
+        psi.data_ptr(), out.data_ptr(), _core.complex_code(psi.dtype), n,
+        psi.numel() >> n, terms.data_ptr(), len(H.terms),
+        _core.stream_of(psi.device))
+    _lib.check(rc, "pauli_sum_apply")
+    return out
+
+
+def pauli_expectation(H: PauliSum, psi: torch.Tensor) -> torch.Tensor:
+    """<psi|H|psi> per state (float64, FP64 accumulation)."""
+    lam = torch.empty_like(psi)
+    _pauli_apply(H, psi.contiguous(), lam)
+    return _real_inner(psi, lam)
+
+
+def _real_inner(a, b):
+    """Re <a|b> per row with the FP64 accumulator returned unrounded."""
+    ip = states._inner_product_kernel(a, b, out_dtype=torch.complex128)
+    return ip.real
+
+
+def _backward_sweep(pc, params, H, psi_L, saved, dtype):
+    n, B = pc.num_qubits, params.shape[0]
+    dev = params.device
+    N = 2 ** n
+    buf = torch.empty(2, B, N, dtype=dtype, device=dev)
+    psi, lam = buf[0], buf[1]
+    psi.copy_(psi_L)
+    _pauli_apply(H, psi, lam)
+    grads = torch.zeros(B, pc.num_params, dtype=torch.float64, device=dev)
+    p = params.detach().contiguous()
+    if p.dtype not in (torch.float32, torch.float64):
+        p = p.to(torch.float64)
+    L = _lib.load()
+    code = _core.complex_code(dtype)
+    acode = _core.real_code(p.dtype)
+    esz = p.element_size()
+    stream = _core.stream_of(dev)
+    nbytes = int(L.gbsv_adjoint_scratch_bytes(B, n))
+    scratch = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=dev)
+    both = buf.view(2 * B, N)
+    segs = pc.segments()
+    for si in range(len(segs) - 1, -1, -1):
+        a, b = segs[si]
+        for op in reversed(pc.ops[a:b]):
+            if op[0] == "rot":
+                _, gen, q, pi, scale = op
+                rc = L.gbsv_adjoint_rotation_step(
+                    psi.data_ptr(), lam.data_ptr(), code, n, B, q, GEN[gen],
+                    p.data_ptr() + pi * esz, acode, pc.num_params, scale,
+                    grads.data_ptr() + pi * 8, pc.num_params, scale,
+                    scratch.data_ptr(), nbytes, stream)
+                _lib.check(rc, "adjoint_rotation_step")
+            else:
+                _, m, qs, _kind = op
+                md = m.conj().T.contiguous().to(device=dev, dtype=dtype)
+                rc = L.gbsv_apply_operator(
+                    both.data_ptr(), both.data_ptr(), code, n, 2 * B, N,
+                    md.data_ptr(), 0, _lib.qubit_array(qs), len(qs), stream)
+                _lib.check(rc, "apply_operator")
+        if saved:
+            psi.copy_(saved[si])  # re-anchor at the forward checkpoint
+    return grads
+
+
+def evaluate(pc: ParamCircuit, params: torch.Tensor, H: PauliSum,
+             psi0: Optional[torch.Tensor] = None,
+             dtype=torch.complex64) -> torch.Tensor:
+    """Forward only: <psi|H|psi> per batch entry (float64), no gradient."""
+    _core.require_cuda(params)
+    psi_L, _ = _forward(pc, params, dtype, psi0, False)
+    return pauli_expectation(H, psi_L)
+
+
+def expectation_and_grad(pc: ParamCircuit, params: torch.Tensor,
+                         H: PauliSum, psi0: Optional[torch.Tensor] = None,
+                         dtype=torch.complex64, checkpoints: bool = True):
+    """(values (B,), grads (B, num_params)), both float64."""
+    _core.require_cuda(params)
+    psi_L, saved = _forward(pc, params, dtype, psi0, checkpoints)
+    values = pauli_expectation(H, psi_L)
+    grads = _backward_sweep(pc, params, H, psi_L, saved, dtype)
+    return values, grads
+
+
+class _Expectation(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, params, pc, H, psi0, dtype, checkpoints):
+        psi_L, saved = _forward(pc, params, dtype, psi0, checkpoints)
+        ctx.pc, ctx.H, ctx.dtype = pc, H, dtype
+        ctx.psi_L, ctx.saved = psi_L, saved
+        ctx.save_for_backward(params)
+        return pauli_expectation(H, psi_L)
+
+    @staticmethod
+    def backward(ctx, g):
+        (params,) = ctx.saved_tensors
+        grads = _backward_sweep(ctx.pc, params, ctx.H, ctx.psi_L, ctx.saved,
+                                ctx.dtype)
+        ctx.psi_L = ctx.saved = None
+        out = (g.to(torch.float64).unsqueeze(-1) * grads).to(params.dtype)
+        return out, None, None, None, None, None
+
+
+def expectation(pc: ParamCircuit, params: torch.Tensor, H: PauliSum,
+                psi0: Optional[torch.Tensor] = None, dtype=torch.complex64,
+                checkpoints: bool = True) -> torch.Tensor:
+    """<psi(params)|H|psi(params)> per batch entry (float64), differentiable
+    with respect to ``params`` by the adjoint method."""
+    _core.require_cuda(params)
+    if params.dim() != 2 or params.shape[1] != pc.num_params:
+        raise ValueError(f"params must be (B, {pc.num_params}), got "
+                         f"{tuple(params.shape)}")
+    return _Expectation.apply(params, pc, H, psi0, dtype, checkpoints)

@@ -186,7 +186,8 @@ def _row_broadcast(a: torch.Tensor, b: torch.Tensor):
     return tuple(out_shape[:-1]), desc, dim, ia, ib
 
 
-def _inner_product_kernel(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+def _inner_product_kernel(a: torch.Tensor, b: torch.Tensor,
+                          out_dtype=None) -> torch.Tensor:
     dev = _core.require_cuda(a, b)
     if a.dtype != b.dtype:
         raise RuntimeError(
@@ -196,14 +197,16 @@ def _inner_product_kernel(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
     a = a.contiguous()
     b = b.contiguous()
     rows_shape, desc, dim, ia, ib = _row_broadcast(a, b)
-    out = torch.empty(rows_shape, dtype=a.dtype, device=dev)
+    out_dtype = a.dtype if out_dtype is None else out_dtype
+    out = torch.empty(rows_shape, dtype=out_dtype, device=dev)
     rows = out.numel()
     if rows == 0:
         return out
     buf, nbytes = _scratch(rows, dim, dev)
     rc = _lib.load().gbsv_inner_product(
         a.data_ptr(), b.data_ptr(), code, desc, dim, ia, ib, out.data_ptr(),
-        code, buf.data_ptr() if buf is not None else None, nbytes,
+        _core.complex_code(out_dtype),
+        buf.data_ptr() if buf is not None else None, nbytes,
         _core.stream_of(dev))
     _lib.check(rc, "inner_product")
     return out

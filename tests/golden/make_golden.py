@@ -205,6 +205,48 @@ def main(ref_root: str) -> None:
         put(name, op=op, state=st, w=w, out=out, gop=op.grad, gstate=st.grad)
         cases.append({"name": name, "kind": "grad", "qubits": qs, "n": n})
 
+    # ---- variational gradient through unitair + torch autograd -----------
+    # ansatz: per layer, on every qubit RZ(phi) then RY(theta) (U = RY RZ),
+    # then a CZ ring; loss = mean_b <sum_i Z_i + 0.5 sum_i X_i X_{i+1}>.
+    # unitair's exp_* return complex64, so the rotation matrices are built
+    # here in float64 (RY(t) = exp_y(t/2), RZ(t) = exp_z(t/2)).
+    n, B, layers = 5, 2, 2
+    params = torch.from_numpy(rng.normal(size=(B, layers, n, 2)))
+    params.requires_grad_()
+    psi = torch.zeros(B, 2 ** n, dtype=torch.complex128)
+    psi[:, 0] = 1
+    cz = torch.diag(torch.tensor([1, 1, 1, -1], dtype=torch.complex128))
+    for l in range(layers):
+        for q in range(n):
+            ph = params[:, l, q, 1] / 2
+            rz = torch.zeros(B, 2, 2, dtype=torch.complex128)
+            rz[:, 0, 0] = torch.exp(-1j * ph)
+            rz[:, 1, 1] = torch.exp(1j * ph)
+            psi = apply_operator(rz, [q], psi)
+            th = params[:, l, q, 0] / 2
+            c, s_ = torch.cos(th), torch.sin(th)
+            ry = torch.stack([torch.stack([c, -s_], -1),
+                              torch.stack([s_, c], -1)], -2).to(
+                                  torch.complex128)
+            psi = apply_operator(ry, [q], psi)
+        for q in range(n):
+            psi = apply_operator(cz, [q, (q + 1) % n], psi)
+    zdiag = torch.zeros(2 ** n, dtype=torch.float64)
+    idx = torch.arange(2 ** n)
+    for q in range(n):
+        zdiag += 1 - 2 * ((idx >> (n - 1 - q)) & 1).to(torch.float64)
+    energy = S.diag_expectation_value(zdiag, psi)
+    xx = torch.tensor([[0, 0, 0, 1], [0, 0, 1, 0], [0, 1, 0, 0],
+                       [1, 0, 0, 0]], dtype=torch.complex128)
+    for q in range(n - 1):
+        energy = energy + 0.5 * S.inner_product(
+            psi, apply_operator(xx, [q, q + 1], psi)).real
+    energy.mean().backward()
+    put("ansatz_grad", params=params.detach(), energy=energy.detach(),
+        grad=params.grad)
+    cases.append({"name": "ansatz_grad", "kind": "ansatz", "n": n,
+                  "layers": layers})
+
     # ---- circuits (canonical generator) -----------------------------------
     for name, n, batch, depth, seed, dtype in (
             ("circ_c64", 12, 4, 200, 0, torch.complex64),

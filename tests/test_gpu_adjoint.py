@@ -1,0 +1,154 @@
+"""Adjoint gradients: against the reference's own autograd (golden vectors),
+central finite differences (h = 1e-3, complex128 forward), and torch
+autograd through the engine's plain per-gate path.  Tolerance: relative
+gradient error <= 1e-4 (the stated target)."""
+import numpy as np
+import pytest
+import torch
+
+import qcware_unitair_gb300 as ug
+from qcware_unitair_gb300.adjoint import (PauliSum, evaluate, expectation,
+                                          expectation_and_grad,
+                                          hardware_efficient_ansatz,
+                                          pauli_expectation)
+from qcware_unitair_gb300.circuits import random_states
+from conftest import golden_data
+
+pytestmark = pytest.mark.gpu
+G = golden_data()
+DEV = torch.device("cuda:0")
+
+
+def tfim(n):
+    H = PauliSum(n)
+    for q in range(n):
+        H.z(q)
+    for q in range(n - 1):
+        H.xx(q, q + 1, 0.5)
+    return H
+
+
+def rel_err(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+
+
+def test_pauli_apply_matches_dense():
+    n = 6
+    H = PauliSum(n).z(0).xx(1, 4, 0.5).add(0.3, {2: "Y", 5: "X"}).add(
+        -1.2, {3: "Y"}).add(0.7, {0: "Z", 5: "Z", 2: "X"})
+    psi = random_states(n, (3,), torch.complex128, seed=1)
+    lam = torch.empty_like(psi).to(DEV)
+    from qcware_unitair_gb300.adjoint import _pauli_apply
+    _pauli_apply(H, psi.to(DEV), lam)
+    ref = psi.numpy() @ H.dense().T
+    assert np.abs(lam.cpu().numpy() - ref).max() < 1e-13
+    e = pauli_expectation(H, psi.to(DEV)).cpu().numpy()
+    ref_e = np.einsum("bi,bi->b", psi.numpy().conj(), ref).real
+    assert np.abs(e - ref_e).max() < 1e-13
+
+
+def test_adjoint_matches_reference_autograd():
+    """Golden: unitair apply_operator + torch autograd (complex128)."""
+    c = G.of_kind("ansatz")[0]
+    n, layers = c["n"], c["layers"]
+    params = torch.from_numpy(G["ansatz_grad/params"]).to(DEV)
+    B = params.shape[0]
+    pc = hardware_efficient_ansatz(n, layers)
+    p = params.reshape(B, -1).clone().requires_grad_()
+    vals = expectation(pc, p, tfim(n), dtype=torch.complex128)
+    assert rel_err(vals.detach().cpu(), G["ansatz_grad/energy"]) < 1e-12
+    vals.mean().backward()
+    ref = G["ansatz_grad/grad"].reshape(B, -1)
+    assert rel_err(p.grad.cpu(), ref) < 1e-10
+    # complex64 state with FP64 accumulation: within the 1e-4 target
+    vals, grads = expectation_and_grad(pc, params.reshape(B, -1).float(),
+                                       tfim(n), dtype=torch.complex64)
+    assert rel_err(grads.cpu() / B, ref) < 1e-4
+
+
+def test_adjoint_vs_finite_differences():
+    n, layers, B = 7, 3, 3
+    pc = hardware_efficient_ansatz(n, layers)
+    rng = np.random.default_rng(0)
+    params = torch.from_numpy(rng.normal(size=(B, pc.num_params))).to(DEV)
+    H = tfim(n)
+    vals, grads = expectation_and_grad(pc, params.float(), H,
+                                       dtype=torch.complex64)
+    h = 1e-3
+    idx = rng.choice(pc.num_params, size=12, replace=False)
+    fd = np.zeros((B, len(idx)))
+    for j, p in enumerate(idx):
+        plus = params.clone()
+        plus[:, p] += h
+        minus = params.clone()
+        minus[:, p] -= h
+        ep = evaluate(pc, plus, H, dtype=torch.complex128)
+        em = evaluate(pc, minus, H, dtype=torch.complex128)
+        fd[:, j] = ((ep - em) / (2 * h)).cpu().numpy()
+    got = grads.cpu().numpy()[:, idx]
+    assert rel_err(got, fd) < 1e-4
+
+
+def test_adjoint_vs_autograd_through_plain_path():
+    """torch autograd through the engine's apply_operator (per-gate
+    kernels with their own backward) gives the same gradient."""
+    n, layers, B = 6, 2, 2
+    pc = hardware_efficient_ansatz(n, layers)
+    rng = np.random.default_rng(4)
+    params = torch.from_numpy(rng.normal(size=(B, pc.num_params))).to(DEV)
+    H = tfim(n)
+    _, grads = expectation_and_grad(pc, params, H, dtype=torch.complex128)
+    p = params.clone().requires_grad_()
+    psi = torch.zeros(B, 2 ** n, dtype=torch.complex128, device=DEV)
+    psi[:, 0] = 1
+    for op in pc.ops:
+        if op[0] == "rot":
+            _, gen, q, pi, scale = op
+            fn = {"X": ug.gates.rx, "Y": ug.gates.ry, "Z": ug.gates.rz}[gen]
+            m = fn(p[:, pi] * scale, dtype=torch.complex128)
+            psi = ug.apply_operator(m, [q], psi)
+        else:
+            psi = ug.apply_operator(op[1].to(DEV), list(op[2]), psi)
+    Hd = torch.from_numpy(H.dense()).to(DEV)
+    e = ug.inner_product(psi, psi @ Hd.T).real
+    e.sum().backward()
+    assert rel_err(p.grad.cpu(), grads.cpu()) < 1e-9
+
+
+def test_c3_full_size_gradients_vs_finite_differences():
+    """20 qubits, batch 256, 12 layers, complex64: adjoint gradients of the
+    batch-mean loss agree with central differences (h = 1e-3, float64) on
+    32 random parameters to <= 1e-4 relative."""
+    if torch.cuda.mem_get_info()[0] < 40 * 2 ** 30:
+        pytest.skip("needs 40 GiB free")
+    n, layers, B = 20, 12, 256
+    pc = hardware_efficient_ansatz(n, layers)
+    g = torch.Generator(device=DEV)
+    g.manual_seed(0)
+    params = torch.randn(B, layers, n, 2, generator=g, device=DEV,
+                         dtype=torch.float32).reshape(B, -1)
+    H = tfim(n)
+    p = params.clone().requires_grad_()
+    loss = expectation(pc, p, H).mean()
+    loss.backward()
+    rng = np.random.default_rng(1)
+    flat = rng.choice(B * pc.num_params, size=32, replace=False)
+    h = 1e-3
+    errs = []
+    for f in flat:
+        b, k = divmod(int(f), pc.num_params)
+        one = params[b:b + 1].to(torch.float64)
+        plus = one.clone()
+        plus[0, k] += h
+        minus = one.clone()
+        minus[0, k] -= h
+        ep = evaluate(pc, plus, H, dtype=torch.complex128)
+        em = evaluate(pc, minus, H, dtype=torch.complex128)
+        fd = float((ep - em)) / (2 * h) / B  # d(mean)/d param
+        ad = float(p.grad[b, k])
+        errs.append((ad, fd))
+    a = np.array(errs)
+    scale = np.abs(a[:, 1]).max()
+    assert np.abs(a[:, 0] - a[:, 1]).max() / scale < 1e-4
