@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0,
                    help="budget of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the adjoint and serving measurements")
     return p.parse_args()
 
 
@@ -196,6 +198,100 @@ def cpu_sample(n: int, gates, budget_s: float):
             "sample": f"first {done} gates of the {n}-qubit circuit, "
                       f"in place, {dt:.1f} s",
             "s_per_gate": dt / done}
+
+
+# ------------------------------------------------- variational gradient ---
+def _tfim(n):
+    from qcware_unitair_gb300.adjoint import PauliSum
+    H = PauliSum(n)
+    for q in range(n):
+        H.z(q)
+    for q in range(n - 1):
+        H.xx(q, q + 1, 0.5)
+    return H
+
+
+def _autograd_plain_loss(pc, p, H, n):
+    """The same loss through torch autograd over the per-gate path."""
+    import torch
+    import qcware_unitair_gb300 as ug
+    B = p.shape[0]
+    psi = torch.zeros(B, 2 ** n, dtype=torch.complex64, device=p.device)
+    psi[:, 0] = 1
+    fns = {"X": ug.gates.rx, "Y": ug.gates.ry, "Z": ug.gates.rz}
+    fixed = {}
+    for op in pc.ops:
+        if op[0] == "rot":
+            _, gen, q, pi, scale = op
+            psi = ug.apply_operator(fns[gen](p[:, pi] * scale), [q], psi)
+        else:
+            key = id(op[1])
+            if key not in fixed:
+                fixed[key] = op[1].to(device=p.device, dtype=torch.complex64)
+            psi = ug.apply_operator(fixed[key], list(op[2]), psi)
+    idx = torch.arange(2 ** n, device=p.device)
+    zdiag = sum(1 - 2 * ((idx >> (n - 1 - q)) & 1).float() for q in range(n))
+    e = ug.diag_expectation_value(zdiag, psi)
+    xx = torch.tensor([[0, 0, 0, 1], [0, 0, 1, 0], [0, 1, 0, 0], [1, 0, 0, 0]],
+                      dtype=torch.complex64, device=p.device)
+    for q in range(n - 1):
+        e = e + 0.5 * ug.inner_product(psi, ug.apply_operator(
+            xx, [q, q + 1], psi)).real
+    return e.mean()
+
+
+def bench_adjoint(dev, n=20, layers=12, batch=256, small_batch=8):
+    """Forward + adjoint backward of the 20-qubit hardware-efficient ansatz
+    (batch 256, 12 layers, complex64, loss = mean <sum Z + 0.5 sum XX>), and
+    the same gradient through torch autograd over the plain per-gate path
+    at a batch whose saved states fit in memory."""
+    import torch
+    from qcware_unitair_gb300.adjoint import (expectation,
+                                              hardware_efficient_ansatz)
+    pc = hardware_efficient_ansatz(n, layers)
+    H = _tfim(n)
+    g = torch.Generator(device=dev)
+    g.manual_seed(0)
+    params = torch.randn(batch, pc.num_params, generator=g, device=dev)
+
+    def adj(pp):
+        p = pp.clone().requires_grad_()
+        expectation(pc, p, H).mean().backward()
+        return p.grad
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps
+
+    t_full = timed(lambda: adj(params), 2)
+    small = params[:small_batch].contiguous()
+    t_adj_small = timed(lambda: adj(small), 3)
+
+    def ag():
+        p = small.clone().requires_grad_()
+        _autograd_plain_loss(pc, p, H, n).backward()
+        return p.grad
+
+    ga = ag()
+    gb = adj(small)
+    agree = float((ga - gb).abs().max() / gb.abs().max())
+    t_ag_small = timed(ag, 2)
+    torch.cuda.empty_cache()
+    return {"workload": f"{n}-qubit hardware-efficient ansatz, {layers} "
+                        f"layers of RY.RZ + CZ ring, complex64, loss mean "
+                        "<sum Z_i + 0.5 sum X_i X_i+1>",
+            "batch": batch, "params": batch * pc.num_params,
+            "s_per_step_forward_backward": round(t_full, 4),
+            "compare_batch": small_batch,
+            "adjoint_s": round(t_adj_small, 4),
+            "autograd_plain_s": round(t_ag_small, 4),
+            "speedup_vs_autograd": round(t_ag_small / t_adj_small, 2),
+            "grad_rel_diff_vs_autograd": agree}
 
 
 # -------------------------------------------------------------- GPU arm ---
@@ -376,6 +472,8 @@ def run_gpu(args, ws, rank, local):
         "gpu_launches": launches,
         "clocks": clocks.summary(),
     }
+    if not args.no_extras:
+        result["adjoint"] = bench_adjoint(dev)
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_sample(n, gates, args.cpu_seconds)
     if rank == 0:

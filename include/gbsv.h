@@ -174,6 +174,74 @@ int gbsv_run_stage_layouts(const void* state_in, void* state_out, int dtype,
                            const void* layouts, int num_layouts,
                            const void* pool, void* stream);
 
+/* Many circuits in one launch: CTA i runs gates[gate_first[i] ..
+ * gate_first[i] + gate_count[i]) (records as for gbsv_run_stage with the
+ * whole state as the tile, i.e. tile bit b = amplitude-index bit b) on the
+ * state of 2^num_qubits amplitudes at state_ptrs[i], in place.  state_ptrs
+ * (uint64), gate_first and gate_count (int32) are device arrays of num_ctas
+ * entries.  num_qubits <= gbsv_fused_max_tile_qubits(dtype).  This is the
+ * batched launch of the serving loop: requests with different circuits and
+ * the same qubit count run together.  No counterpart in unitair, which
+ * applies one operator to one batch at a time. */
+int gbsv_run_programs(int dtype, int num_qubits, int num_ctas,
+                      const void* state_ptrs, const void* gate_first,
+                      const void* gate_count, const void* gates,
+                      const void* pool, void* stream);
+
+/* ---- host-side circuit planner ------------------------------------------ */
+
+/* One gate of a circuit to plan (host memory).  kind: 0 dense, 1 diagonal,
+ * 2 controlled-U (4x4 of the form diag(I, U), the first qubit controls).
+ * Its row-major 2^nq x 2^nq complex128 matrix is at matrices + mat
+ * (+ b * mat_bstride for per-state copy b of num_batch). */
+typedef struct gbsv_gate_desc {
+  int32_t kind;
+  int32_t nq;
+  int32_t q0, q1;
+  int64_t mat;
+  int64_t mat_bstride;
+  int64_t num_batch;
+} gbsv_gate_desc_t;
+
+/* One pass of a planned circuit.  type 0: a single unfused gate (first =
+ * gate index); 1: a shared-memory stage (records [first, first+count));
+ * 2: a register-blocked stage (layouts [first, first+count)).  positions
+ * are the stage's tile bits (the first `contiguous` are 0..contiguous-1). */
+typedef struct gbsv_plan_op {
+  int32_t type;
+  int32_t contiguous;
+  int32_t first, count;
+  int32_t positions[16];
+} gbsv_plan_op_t;
+
+/* Caller-owned output buffers of gbsv_plan (host memory) and their counts. */
+typedef struct gbsv_plan {
+  int32_t dtype;          /* pool element type, GBSV_C64 or GBSV_C128 */
+  int32_t used_layouts;   /* 1 if stages are register-blocked */
+  gbsv_plan_op_t* ops;
+  int32_t max_ops, num_ops;
+  gbsv_fused_gate_t* records;
+  int32_t max_records, num_records;
+  gbsv_layout_t* layouts;
+  int32_t max_layouts, num_layouts;
+  void* pool;
+  int64_t max_pool, pool_len;
+} gbsv_plan_t;
+
+/* Plan a circuit into fused stages on the host: greedy stages of
+ * tile_qubits tile bits (the lowest min_contiguous always included),
+ * register layouts of register_bits bits when the tile allows (0 = plain
+ * shared-memory stages), gate
+ * records specialised by structure, and the matrix pool converted to
+ * plan->dtype.  fuse == 0 plans one pass per gate.  Returns
+ * GBSV_ERR_SCRATCH if an output buffer is too small.  This is the native
+ * counterpart of the planner in fusion.py (same output), fast enough to run
+ * per request in the serving loop.  No counterpart in unitair. */
+int gbsv_plan(const gbsv_gate_desc_t* gates, int num_gates,
+              const void* matrices, int num_qubits, int tile_qubits,
+              int min_contiguous, int register_bits, int fuse,
+              gbsv_plan_t* plan);
+
 /* ---- gradients --------------------------------------------------------- */
 
 /* Scratch bytes gbsv_operator_grad needs (0 = none). */

@@ -40,6 +40,24 @@ class Bcast(ctypes.Structure):
     ]
 
 
+class PlanOp(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("contiguous", ctypes.c_int32),
+                ("first", ctypes.c_int32), ("count", ctypes.c_int32),
+                ("positions", ctypes.c_int32 * 16)]
+
+
+class Plan(ctypes.Structure):
+    _fields_ = [("dtype", ctypes.c_int32), ("used_layouts", ctypes.c_int32),
+                ("ops", ctypes.c_void_p), ("max_ops", ctypes.c_int32),
+                ("num_ops", ctypes.c_int32),
+                ("records", ctypes.c_void_p), ("max_records", ctypes.c_int32),
+                ("num_records", ctypes.c_int32),
+                ("layouts", ctypes.c_void_p), ("max_layouts", ctypes.c_int32),
+                ("num_layouts", ctypes.c_int32),
+                ("pool", ctypes.c_void_p), ("max_pool", ctypes.c_int64),
+                ("pool_len", ctypes.c_int64)]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _I32 = ctypes.c_int32
@@ -65,6 +83,9 @@ SIGNATURES = {
     "gbsv_run_stage_layouts": (_I, [_P, _P, _I, _I, _I64, _I64, _I, _I,
                                     ctypes.POINTER(_I32), _P, _P, _I, _P,
                                     _P]),
+    "gbsv_run_programs": (_I, [_I, _I, _I, _P, _P, _P, _P, _P, _P]),
+    "gbsv_plan": (_I, [_P, _I, _P, _I, _I, _I, _I, _I,
+                       ctypes.POINTER(Plan)]),
     "gbsv_operator_grad_scratch_bytes": (_SZ, [_I64, _I, _I, _I]),
     "gbsv_operator_grad": (_I, [_P, _P, _I, _I, _I64, _I64,
                                 ctypes.POINTER(_I32), _I, _P, _I, _P, _SZ,

@@ -210,7 +210,8 @@ def _initial_state(n, B, dtype, device, psi0):
     return s.reshape(B, 2 ** n).contiguous()
 
 
-def _forward(pc: ParamCircuit, params, dtype, psi0, checkpoints: bool):
+def _forward(pc: ParamCircuit, params, dtype, psi0, checkpoints: bool,
+             fuse: bool = True):
     """Run the circuit; return (psi_L, [psi at each segment start])."""
     n, B = pc.num_qubits, params.shape[0]
     dev = params.device
@@ -220,8 +221,8 @@ def _forward(pc: ParamCircuit, params, dtype, psi0, checkpoints: bool):
         if checkpoints:
             saved.append(psi.clone())
         if b > a:
-            prog = pc._segment_circuit(a, b, params, dtype).compile(dtype,
-                                                                    dev)
+            prog = pc._segment_circuit(a, b, params, dtype).compile(
+                dtype, dev, fuse=fuse)
             prog.run(psi, inplace=True)
     return psi, saved
 
@@ -306,10 +307,12 @@ def evaluate(pc: ParamCircuit, params: torch.Tensor, H: PauliSum,
 
 def expectation_and_grad(pc: ParamCircuit, params: torch.Tensor,
                          H: PauliSum, psi0: Optional[torch.Tensor] = None,
-                         dtype=torch.complex64, checkpoints: bool = True):
-    """(values (B,), grads (B, num_params)), both float64."""
+                         dtype=torch.complex64, checkpoints: bool = True,
+                         fuse: bool = True):
+    """(values (B,), grads (B, num_params)), both float64.  ``fuse=False``
+    runs the forward pass one kernel per gate."""
     _core.require_cuda(params)
-    psi_L, saved = _forward(pc, params, dtype, psi0, checkpoints)
+    psi_L, saved = _forward(pc, params, dtype, psi0, checkpoints, fuse)
     values = pauli_expectation(H, psi_L)
     grads = _backward_sweep(pc, params, H, psi_L, saved, dtype)
     return values, grads

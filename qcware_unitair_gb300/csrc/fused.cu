@@ -102,50 +102,25 @@ __device__ __forceinline__ void load_gate_chunk(SGate<C>* sg,
   }
 }
 
+// Apply gates[0 .. num_gates) to the tile S (2^m amplitudes, swizzled for
+// complex64) of state s whose base index is `base`; gates on bits outside
+// the tile become per-tile factors accumulated into tscale.
 template <typename R>
-__global__ void __launch_bounds__(512, 2)
-    fused_stage_kernel(const Cx<R>* in, Cx<R>* out, const Cx<R>* pool,
-                       StageArgs a) {
+__device__ __forceinline__ void run_gates_smem(Cx<R>* S, int M, uint64_t base,
+                                               uint64_t s,
+                                               const FusedGate* gates,
+                                               int num_gates,
+                                               const Cx<R>* pool,
+                                               Cx<R>& tscale, bool& scaled) {
   using C = Cx<R>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  C* S = reinterpret_cast<C*>(smem_raw);
+  constexpr int PER = 16 / sizeof(C);
   const int T = blockDim.x;
   const int tid = threadIdx.x;
-  const int M = 1 << a.m;
-  const int run = 1 << a.c;
-  const uint64_t tiles_per_state = uint64_t(1) << (a.n - a.m);
-  const uint64_t s = blockIdx.x / tiles_per_state;
-  uint64_t base = blockIdx.x % tiles_per_state;
-  for (int j = 0; j < a.m; ++j) base = insert_zero(base, a.spos[j]);
-
-  const C* src = in + s * a.in_stride + base;
-  C* dst = out + (s << a.n) + base;
-
-  // ---- load: 16-byte pieces; a piece never crosses a run --------------
-  constexpr int PER = 16 / sizeof(C);  // amplitudes per 16-byte piece
-  for (int l = tid * PER; l < M; l += T * PER) {
-    const int r = l >> a.c;
-    uint64_t off = (uint64_t)(l & (run - 1));
-    for (int j = 0; j < a.m - a.c; ++j)
-      if ((r >> j) & 1) off += uint64_t(1) << a.hpos[j];
-    if constexpr (PER == 2)
-      cp_async16<R>(&S[swz(l)], src + off);
-    else
-      cp_async16<R>(&S[l], src + off);
-  }
-  cp_async_wait_all();
-  __syncthreads();
-
-  C tscale;
-  tscale.x = 1;
-  tscale.y = 0;
-  bool scaled = false;
-
   __shared__ SGate<C> sg[GCHUNK];
-  for (int c0 = 0; c0 < a.num_gates; c0 += GCHUNK) {
-    const int cnt = min(GCHUNK, a.num_gates - c0);
+  for (int c0 = 0; c0 < num_gates; c0 += GCHUNK) {
+    const int cnt = min(GCHUNK, num_gates - c0);
     if (c0 > 0) __syncthreads();
-    load_gate_chunk<C>(sg, a.gates, pool, s, c0, cnt);
+    load_gate_chunk<C>(sg, gates, pool, s, c0, cnt);
     __syncthreads();
     for (int gi = 0; gi < cnt; ++gi) {
       const SGate<C>& g = sg[gi];
@@ -224,6 +199,50 @@ __global__ void __launch_bounds__(512, 2)
       __syncthreads();
     }
   }
+
+}
+
+template <typename R>
+__global__ void __launch_bounds__(512, 2)
+    fused_stage_kernel(const Cx<R>* in, Cx<R>* out, const Cx<R>* pool,
+                       StageArgs a) {
+  using C = Cx<R>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* S = reinterpret_cast<C*>(smem_raw);
+  const int T = blockDim.x;
+  const int tid = threadIdx.x;
+  const int M = 1 << a.m;
+  const int run = 1 << a.c;
+  const uint64_t tiles_per_state = uint64_t(1) << (a.n - a.m);
+  const uint64_t s = blockIdx.x / tiles_per_state;
+  uint64_t base = blockIdx.x % tiles_per_state;
+  for (int j = 0; j < a.m; ++j) base = insert_zero(base, a.spos[j]);
+
+  const C* src = in + s * a.in_stride + base;
+  C* dst = out + (s << a.n) + base;
+
+  // ---- load: 16-byte pieces; a piece never crosses a run --------------
+  constexpr int PER = 16 / sizeof(C);  // amplitudes per 16-byte piece
+  for (int l = tid * PER; l < M; l += T * PER) {
+    const int r = l >> a.c;
+    uint64_t off = (uint64_t)(l & (run - 1));
+    for (int j = 0; j < a.m - a.c; ++j)
+      if ((r >> j) & 1) off += uint64_t(1) << a.hpos[j];
+    if constexpr (PER == 2)
+      cp_async16<R>(&S[swz(l)], src + off);
+    else
+      cp_async16<R>(&S[l], src + off);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+
+  C tscale;
+  tscale.x = 1;
+  tscale.y = 0;
+  bool scaled = false;
+
+  run_gates_smem<R>(S, M, base, s, a.gates, a.num_gates, pool, tscale,
+                    scaled);
 
   // ---- store --------------------------------------------------------
   for (int l = tid * PER; l < M; l += T * PER) {
@@ -852,4 +871,105 @@ extern "C" int gbsv_run_stage_layouts(
         a);
   }
   return after_launch("fused_reg_kernel");
+}
+
+// ---------------------------------------------------------------------------
+// Many programs in one launch: CTA i owns one whole state of 2^n <= 2^14
+// amplitudes (a single tile) at states[i] and runs its own gate list
+// gates[first[i] .. first[i] + count[i]) on it in shared memory.  Requests
+// with different circuits but the same qubit count share one launch.
+namespace gbsv {
+
+template <typename R>
+__global__ void __launch_bounds__(512, 2)
+    multi_program_kernel(int n, const unsigned long long* states,
+                         const int32_t* first, const int32_t* count,
+                         const FusedGate* gates, const Cx<R>* pool) {
+  using C = Cx<R>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* S = reinterpret_cast<C*>(smem_raw);
+  const int M = 1 << n;
+  const int T = blockDim.x;
+  const int tid = threadIdx.x;
+  C* st = reinterpret_cast<C*>(states[blockIdx.x]);
+  constexpr int PER = 16 / sizeof(C);
+  for (int l = tid * PER; l < M; l += T * PER)
+    cp_async16<R>(&S[PER == 2 ? swz(l) : l], st + l);
+  cp_async_wait_all();
+  __syncthreads();
+  C tscale;
+  tscale.x = 1;
+  tscale.y = 0;
+  bool scaled = false;
+  run_gates_smem<R>(S, M, 0, 0, gates + first[blockIdx.x], count[blockIdx.x],
+                    pool, tscale, scaled);
+  for (int l = tid * PER; l < M; l += T * PER) {
+    const int pl = PER == 2 ? swz(l) : l;
+    C v0 = S[pl];
+    if (scaled) v0 = cmul(tscale, v0);
+    if constexpr (PER == 2) {
+      C v1 = S[pl + 1];
+      if (scaled) v1 = cmul(tscale, v1);
+      __stcs(reinterpret_cast<float4*>(st + l),
+             make_float4(v0.x, v0.y, v1.x, v1.y));
+    } else {
+      __stcs(st + l, v0);
+    }
+  }
+}
+
+}  // namespace gbsv
+
+extern "C" int gbsv_run_programs(int dtype, int num_qubits, int num_ctas,
+                                 const void* state_ptrs,
+                                 const void* gate_first,
+                                 const void* gate_count, const void* gates,
+                                 const void* pool, void* stream) {
+  if (dtype != GBSV_C64 && dtype != GBSV_C128)
+    return set_error(GBSV_ERR_INVALID_ARG, "state dtype must be complex");
+  const int mmax = gbsv_fused_max_tile_qubits(dtype);
+  const int nmin = dtype == GBSV_C64 ? 1 : 0;
+  if (num_qubits < nmin || num_qubits > mmax || num_ctas < 0)
+    return set_error(GBSV_ERR_INVALID_ARG,
+                     "run_programs needs %d <= qubits <= %d (got %d)", nmin,
+                     mmax, num_qubits);
+  if (num_ctas == 0) return GBSV_OK;
+  if (!state_ptrs || !gate_first || !gate_count || !gates || !pool)
+    return set_error(GBSV_ERR_INVALID_ARG, "null pointer");
+  const int amp = dtype_bytes(dtype);
+  const size_t smem = (size_t)amp << num_qubits;
+  int threads = (1 << num_qubits) / 4;
+  if (threads > 512) threads = 512;
+  if (threads < 32) threads = 32;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (dtype == GBSV_C64) {
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(multi_program_kernel<float>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(sizeof(float2) << mmax));
+      attr = true;
+    }
+    multi_program_kernel<float><<<num_ctas, threads, smem, st>>>(
+        num_qubits, static_cast<const unsigned long long*>(state_ptrs),
+        static_cast<const int32_t*>(gate_first),
+        static_cast<const int32_t*>(gate_count),
+        static_cast<const FusedGate*>(gates),
+        static_cast<const float2*>(pool));
+  } else {
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(multi_program_kernel<double>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(sizeof(double2) << mmax));
+      attr = true;
+    }
+    multi_program_kernel<double><<<num_ctas, threads, smem, st>>>(
+        num_qubits, static_cast<const unsigned long long*>(state_ptrs),
+        static_cast<const int32_t*>(gate_first),
+        static_cast<const int32_t*>(gate_count),
+        static_cast<const FusedGate*>(gates),
+        static_cast<const double2*>(pool));
+  }
+  return after_launch("multi_program_kernel");
 }

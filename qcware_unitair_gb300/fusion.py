@@ -151,9 +151,9 @@ class Circuit:
     def compile(self, dtype=torch.complex64, device="cuda", fuse=True,
                 tile_qubits: Optional[int] = None,
                 min_contiguous: Optional[int] = None,
-                layouts: bool = True) -> "Program":
+                layouts: bool = True, native: bool = True) -> "Program":
         return Program(self, dtype, torch.device(device), fuse, tile_qubits,
-                       min_contiguous, layouts)
+                       min_contiguous, layouts, native)
 
     def run(self, state: torch.Tensor, fuse: bool = True,
             inplace: bool = False) -> torch.Tensor:
@@ -269,6 +269,17 @@ def _dense1_kind(u) -> Tuple[int, int]:
     if _is_real(u):
         return FG_REAL1, 0
     return FG_DENSE1, 0
+
+
+def _to_device(arr: Optional[np.ndarray], dev) -> torch.Tensor:
+    """One pinned, non-blocking host-to-device copy (no host stall behind
+    work already queued on the stream)."""
+    if arr is None:
+        return torch.zeros(64, dtype=torch.uint8, device=dev)
+    t = torch.from_numpy(np.ascontiguousarray(arr).reshape(-1).copy())
+    if dev.type == "cuda":
+        t = t.pin_memory()
+    return t.to(dev, non_blocking=True)
 
 
 def _record(g: CircuitGate, n: int, local: dict, kreg: Optional[dict],
@@ -387,11 +398,63 @@ def _plan_layouts(gates, n, local, m, rb):
     return layouts
 
 
+DESC_DTYPE = np.dtype([("kind", "<i4"), ("nq", "<i4"), ("q0", "<i4"),
+                       ("q1", "<i4"), ("mat", "<i8"), ("mat_bstride", "<i8"),
+                       ("num_batch", "<i8")])
+PLANOP_DTYPE = np.dtype([("type", "<i4"), ("contiguous", "<i4"),
+                         ("first", "<i4"), ("count", "<i4"),
+                         ("positions", "<i4", (16,))])
+_KIND_CODE = {DENSE: 0, DIAG: 1, CTRL: 2}
+
+
+def native_plan(gates: Sequence[CircuitGate], n: int, m: int, c_min: int,
+                rb: int, fuse: bool, dtype) -> Optional[dict]:
+    """Plan with gbsv_plan (C++).  None when a matrix lives on the device
+    (reading it would need a sync; the Python planner handles that)."""
+    G = len(gates)
+    if any(g.matrix.is_cuda for g in gates):
+        return None
+    desc = np.zeros(G, dtype=DESC_DTYPE)
+    parts = []
+    off = 0
+    for i, g in enumerate(gates):
+        mat = g.matrix.detach().numpy().astype(np.complex128, copy=False)
+        d = mat.shape[-1]
+        desc[i] = (_KIND_CODE[g.kind], len(g.qubits), g.qubits[0],
+                   g.qubits[1] if len(g.qubits) > 1 else 0, off,
+                   d * d if mat.ndim == 3 else 0,
+                   mat.shape[0] if mat.ndim == 3 else 1)
+        parts.append(mat.reshape(-1))
+        off += mat.size
+    mats = np.ascontiguousarray(np.concatenate(parts)) if parts else \
+        np.zeros(1, np.complex128)
+    cdt = np.complex64 if dtype == torch.complex64 else np.complex128
+    max_pool = max(16, sum(16 * max(1, int(x)) for x in desc["num_batch"]))
+    ops = np.zeros(max(1, G), dtype=PLANOP_DTYPE)
+    recs = np.zeros(max(1, G), dtype=FG_DTYPE)
+    lays = np.zeros(max(1, G), dtype=LAYOUT_DTYPE)
+    pool = np.zeros(max_pool, dtype=cdt)
+    pl = _lib.Plan()
+    pl.dtype = _core.complex_code(dtype)
+    pl.ops, pl.max_ops = ops.ctypes.data, len(ops)
+    pl.records, pl.max_records = recs.ctypes.data, len(recs)
+    pl.layouts, pl.max_layouts = lays.ctypes.data, len(lays)
+    pl.pool, pl.max_pool = pool.ctypes.data, len(pool)
+    rc = _lib.load().gbsv_plan(desc.ctypes.data, G, mats.ctypes.data, n, m,
+                               c_min, rb, int(bool(fuse)), ctypes.byref(pl))
+    _lib.check(rc, "plan")
+    return {"ops": ops[:pl.num_ops], "records": recs[:pl.num_records],
+            "layouts": lays[:pl.num_layouts], "pool": pool[:pl.pool_len],
+            "used_layouts": bool(pl.used_layouts)}
+
+
 class Program:
     """A compiled circuit for one dtype/device (see module doc)."""
 
     def __init__(self, circuit: Circuit, dtype, device, fuse=True,
-                 tile_qubits=None, min_contiguous=None, layouts=True):
+                 tile_qubits=None, min_contiguous=None, layouts=True,
+                 native=True):
+        self.native = False
         self.n = n = circuit.num_qubits
         self.dtype = dtype
         self.device = device
@@ -417,11 +480,52 @@ class Program:
                     raise ValueError("per-state gates must share one batch "
                                      "size")
                 self.batch = b
+        nat = None
+        if native:
+            nat = native_plan(circuit.gates, n, self.m, self.c_min,
+                              self.rb if self.use_layouts else 0, fuse, dtype)
+        if nat is not None and nat["used_layouts"] == self.use_layouts:
+            self._build_native(nat, circuit.gates)
+            return
         if fuse:
             raw = plan(circuit.gates, n, self.m, self.c_min)
         else:
             raw = [("plain", g) for g in circuit.gates]
         self._build(raw)
+
+    def _build_native(self, nat, gates):
+        dev, dt = self.device, self.dtype
+        self.ops = []
+        for op in nat["ops"]:
+            t, c, first, count = (int(op["type"]), int(op["contiguous"]),
+                                  int(op["first"]), int(op["count"]))
+            if t == 0:
+                g = gates[first]
+                mat = g.matrix.to(dtype=dt).contiguous()
+                if dev.type == "cuda":
+                    mat = mat.pin_memory()
+                self.ops.append(("plain", mat.to(dev, non_blocking=True),
+                                 g.qubits))
+                continue
+            positions = (ctypes.c_int32 * self.m)(
+                *[int(x) for x in op["positions"][:self.m]])
+            self.ops.append(("layouts" if t == 2 else "stage", c, positions,
+                             first, count))
+        recs, lays = nat["records"], nat["layouts"]
+        self.gate_records = _to_device(recs.view(np.uint8) if len(recs)
+                                       else None, dev)
+        self.layout_records = _to_device(lays.view(np.uint8) if len(lays)
+                                         else None, dev)
+        self.num_layouts = len(lays)
+        pool = torch.from_numpy(nat["pool"]) if len(nat["pool"]) else \
+            torch.zeros(1, dtype=dt)
+        if dev.type == "cuda":
+            pool = pool.pin_memory()
+        self._staging = pool
+        self.pool = pool.to(dev, non_blocking=True)
+        self.num_stages = sum(1 for o in self.ops if o[0] != "plain")
+        self.num_plain = sum(1 for o in self.ops if o[0] == "plain")
+        self.native = True
 
     # -- packing ---------------------------------------------------------
     def _build(self, raw):
@@ -432,23 +536,23 @@ class Program:
         pool_len = 0
 
         def add_pool(values: torch.Tensor):
-            """values (nv,) or (B, nv) -> (offset, bstride)."""
+            """values (nv,) or (B, nv) -> (offset, bstride).  Host values
+            stay on the host until one transfer at the end."""
             nonlocal pool_len
-            v = values.to(device=dev, dtype=dt)
+            v = values.to(dtype=dt)
             off = pool_len
-            if v.dim() == 2:
-                pool_parts.append(v.reshape(-1))
-                pool_len += v.numel()
-                return off, v.shape[1]
-            pool_parts.append(v)
+            pool_parts.append(v.reshape(-1))
             pool_len += v.numel()
-            return off, 0
+            return off, (v.shape[1] if v.dim() == 2 else 0)
 
         self.ops = []
         for kind, item in raw:
             if kind == "plain":
                 g = item
-                mat = g.matrix.to(device=dev, dtype=dt).contiguous()
+                mat = g.matrix.to(dtype=dt).contiguous()
+                if dev.type == "cuda" and not mat.is_cuda:
+                    mat = mat.pin_memory()
+                mat = mat.to(dev, non_blocking=True)
                 self.ops.append(("plain", mat, g.qubits))
                 continue
             st: _Stage = item
@@ -484,22 +588,21 @@ class Program:
                 rec["mat"], rec["mat_bstride"] = off, bstride
                 records.append(rec)
             self.ops.append(("stage", c, positions, first, len(st.gates)))
-        if records:
-            arr = np.stack(records)
-            self.gate_records = torch.from_numpy(
-                arr.view(np.uint8).copy()).to(dev)
-        else:
-            self.gate_records = torch.empty(0, dtype=torch.uint8, device=dev)
-        if layouts:
-            arr = np.stack(layouts)
-            self.layout_records = torch.from_numpy(
-                arr.view(np.uint8).copy()).to(dev)
-        else:
-            self.layout_records = torch.empty(0, dtype=torch.uint8,
-                                              device=dev)
+        self.gate_records = _to_device(
+            np.stack(records).view(np.uint8) if records else None, dev)
+        self.layout_records = _to_device(
+            np.stack(layouts).view(np.uint8) if layouts else None, dev)
         self.num_layouts = len(layouts)
-        self.pool = torch.cat(pool_parts) if pool_parts else torch.zeros(
-            1, dtype=dt, device=dev)
+        if not pool_parts:
+            self.pool = torch.zeros(1, dtype=dt, device=dev)
+        elif all(not p.is_cuda for p in pool_parts):
+            host = torch.cat(pool_parts)
+            if dev.type == "cuda":
+                host = host.pin_memory()
+            self.pool = host.to(dev, non_blocking=True)
+            self._staging = host  # alive until the copy has run
+        else:
+            self.pool = torch.cat([p.to(dev) for p in pool_parts])
         self.num_stages = sum(1 for o in self.ops if o[0] != "plain")
         self.num_plain = sum(1 for o in self.ops if o[0] == "plain")
 

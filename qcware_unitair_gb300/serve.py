@@ -1,0 +1,341 @@
+"""Continuous-batching circuit server.
+
+Requests (a circuit of the canonical gate set on n qubits, a batch of
+seeded random initial states, optionally adjoint gradients of <Z_0>) arrive
+over time.  One host loop runs four things while earlier work is still on
+the GPU:
+
+  admission   FIFO by arrival; a request is admitted when its HBM footprint
+              fits the byte budget (160 GB by default).  If the head of the
+              queue does not fit, later requests may pass it only until it
+              has waited ``reserve_after`` seconds; from then on admission
+              waits for memory, so large requests are not starved.
+  packing     admitted requests whose states fit one tile (n <= 13 for
+              complex64) are packed, whatever their circuits, into ONE
+              multi-program launch per qubit count (gbsv_run_programs: one
+              CTA per state, each running its own gate list).
+  streams     larger requests run as fused programs on a pool of CUDA
+              streams, so several requests' kernels overlap on the device.
+  completion  CUDA events are polled; finished requests return norms and
+              <Z_0> (FP64 reductions) and free their memory for the next
+              admissions.
+
+``serve_plain`` is the baseline: the same trace, FIFO, one request at a
+time, one kernel per gate on one stream.  Both return one ``Result`` per
+request with arrival, admission and completion times.
+"""
+from __future__ import annotations
+
+import collections
+import math
+import time
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _core, _lib, simulation, states
+from .circuits import Gate, random_circuit, ROTATIONS
+from .fusion import Circuit, FG_DTYPE, _record
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival: float
+    num_qubits: int
+    num_states: int
+    gates: List[Gate]
+    want_grad: bool = False
+    seed: int = 0
+
+    @property
+    def state_bytes(self) -> int:
+        return self.num_states * (8 << self.num_qubits)
+
+    @property
+    def footprint(self) -> int:
+        # gradients keep psi, lambda and up to ~sqrt(depth) checkpoints
+        return self.state_bytes * (6 if self.want_grad else 1)
+
+
+@dataclass
+class Result:
+    rid: int
+    norms: np.ndarray
+    z0: np.ndarray
+    grads: Optional[np.ndarray]
+    arrival: float
+    admitted: float
+    done: float
+    final: Optional[torch.Tensor] = None
+
+    @property
+    def latency(self) -> float:
+        return self.done - self.arrival
+
+
+def make_trace(num_requests: int = 20000, rate: float = 50.0, seed: int = 0,
+               qubits=(10, 28), depth=(20, 500), batch=(1, 64),
+               grad_fraction: float = 0.2) -> List[Request]:
+    """Poisson arrivals at ``rate`` per second; qubits, depth and states
+    uniform in the given inclusive ranges; gates from the canonical set."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(num_requests):
+        t += float(rng.exponential(1.0 / rate))
+        n = int(rng.integers(qubits[0], qubits[1] + 1))
+        d = int(rng.integers(depth[0], depth[1] + 1))
+        b = int(rng.integers(batch[0], batch[1] + 1))
+        g = bool(rng.random() < grad_fraction)
+        out.append(Request(i, t, n, b, random_circuit(n, d, seed=seed * 1000003
+                                                      + i), g, seed + i))
+    return out
+
+
+def summarize(results: Sequence[Result]) -> dict:
+    lat = np.array([r.latency for r in results])
+    t0 = min(r.arrival for r in results)
+    t1 = max(r.done for r in results)
+    return {"requests": len(results),
+            "circuits_per_s": round(len(results) / (t1 - t0), 3),
+            "p50_s": round(float(np.percentile(lat, 50)), 4),
+            "p99_s": round(float(np.percentile(lat, 99)), 4),
+            "mean_s": round(float(lat.mean()), 4),
+            "makespan_s": round(t1 - t0, 3)}
+
+
+# ---------------------------------------------------------------- helpers --
+def _init_states(req: Request, device, dtype=torch.complex64):
+    g = torch.Generator(device=device)
+    g.manual_seed(int(req.seed))
+    psi = torch.randn(req.num_states, 2 ** req.num_qubits, dtype=dtype,
+                      device=device, generator=g)
+    psi /= states.norm_squared(psi).sqrt().unsqueeze(-1)
+    return psi
+
+
+def _outputs(psi: torch.Tensor, n: int):
+    """FP64 norms and <Z_0> (qubit 0 is the top index bit: <Z_0> is the
+    weight of the first half minus that of the second)."""
+    B = psi.shape[0]
+    halves = states.norm_squared_fp64(psi.view(B * 2, 2 ** (n - 1)))
+    halves = halves.view(B, 2)
+    return halves.sum(-1), halves[:, 0] - halves[:, 1]
+
+
+def _grad_circuit(req: Request):
+    """ParamCircuit with one parameter per rotation (angles shared by the
+    request's states) and <Z_0> as the observable."""
+    from .adjoint import ParamCircuit, PauliSum
+    rots = [g for g in req.gates if g.name in ROTATIONS]
+    pc = ParamCircuit(req.num_qubits, max(1, len(rots)))
+    angles = []
+    for g in req.gates:
+        if g.name in ROTATIONS:
+            {"RX": pc.rx, "RY": pc.ry, "RZ": pc.rz}[g.name](
+                g.qubits[0], len(angles))
+            angles.append(g.theta)
+        else:
+            pc.gate(g.matrix(), g.qubits)
+    return pc, PauliSum(req.num_qubits).z(0), angles
+
+
+def _run_grad(req: Request, psi0: torch.Tensor, fuse: bool = True):
+    from .adjoint import expectation_and_grad
+    pc, H, angles = _grad_circuit(req)
+    dev = psi0.device
+    params = torch.tensor(angles or [0.0], dtype=torch.float64)
+    params = params.pin_memory().to(dev, non_blocking=True).expand(
+        req.num_states, -1).contiguous()
+    _, grads = expectation_and_grad(pc, params, H, psi0=psi0, fuse=fuse)
+    return grads
+
+
+# ----------------------------------------------------------------- server --
+class Server:
+    def __init__(self, device="cuda", budget_bytes: float = 160e9,
+                 num_streams: int = 4, reserve_after: float = 0.5,
+                 keep_states: bool = False):
+        self.device = torch.device(device)
+        self.budget = float(budget_bytes)
+        self.streams = [torch.cuda.Stream(self.device)
+                        for _ in range(num_streams)]
+        self.reserve_after = reserve_after
+        self.keep_states = keep_states
+        L = _lib.load()
+        self.small_max = int(L.gbsv_fused_max_tile_qubits(_lib.C64))
+        self._next_stream = 0
+        self.peak_used = 0.0  # largest admitted footprint seen (bytes)
+
+    def _stream(self):
+        s = self.streams[self._next_stream % len(self.streams)]
+        self._next_stream += 1
+        return s
+
+    # -- launches ---------------------------------------------------------
+    def _launch_small(self, reqs):
+        """Requests with one qubit count -> one packed launch."""
+        n = reqs[0].num_qubits
+        stream = self._stream()
+        with torch.cuda.stream(stream):
+            items = [(req, _init_states(req, self.device)) for req in reqs]
+        recs, pool_parts, first, count, ptrs = [], [], [], [], []
+        pool_len = 0
+        local = {p: p for p in range(n)}
+        for req, psi in items:
+            f0 = len(recs)
+            for g in Circuit.from_gates(n, req.gates).gates:
+                rec, vals = _record(g, n, local, None)
+                v = vals.reshape(-1).to(torch.complex64)
+                rec["mat"], rec["mat_bstride"] = pool_len, 0
+                pool_parts.append(v)
+                pool_len += v.numel()
+                recs.append(rec)
+            N = 2 ** n
+            base = psi.data_ptr()
+            for j in range(req.num_states):
+                ptrs.append(base + j * N * 8)
+                first.append(f0)
+                count.append(len(recs) - f0)
+        dev = self.device
+        with torch.cuda.stream(stream):
+            gates = torch.from_numpy(np.stack(recs).view(np.uint8).copy()) \
+                if recs else torch.zeros(48, dtype=torch.uint8)
+            pool = torch.cat(pool_parts) if pool_parts else \
+                torch.zeros(1, dtype=torch.complex64)
+            gates = gates.pin_memory().to(dev, non_blocking=True)
+            pool = pool.pin_memory().to(dev, non_blocking=True)
+            meta = torch.tensor(ptrs, dtype=torch.int64).pin_memory().to(
+                dev, non_blocking=True)
+            fi = torch.tensor(first, dtype=torch.int32).pin_memory().to(
+                dev, non_blocking=True)
+            co = torch.tensor(count, dtype=torch.int32).pin_memory().to(
+                dev, non_blocking=True)
+            rc = _lib.load().gbsv_run_programs(
+                _lib.C64, n, len(ptrs), meta.data_ptr(), fi.data_ptr(),
+                co.data_ptr(), gates.data_ptr(), pool.data_ptr(),
+                stream.cuda_stream)
+            _lib.check(rc, "run_programs")
+            outs = [(req, psi, _outputs(psi, n)) for req, psi in items]
+            ev = torch.cuda.Event()
+            ev.record(stream)
+        keep = (gates, pool, meta, fi, co)
+        return [(ev, req, psi, o, None, keep) for req, psi, o in outs]
+
+    def _launch_large(self, req):
+        stream = self._stream()
+        with torch.cuda.stream(stream):
+            psi = _init_states(req, self.device)
+            grads = None
+            if req.want_grad:
+                grads = _run_grad(req, psi.clone())
+            prog = Circuit.from_gates(req.num_qubits, req.gates).compile(
+                torch.complex64, self.device)
+            prog.run(psi, inplace=True)
+            o = _outputs(psi, req.num_qubits)
+            ev = torch.cuda.Event()
+            ev.record(stream)
+        return (ev, req, psi, o, grads, prog)
+
+    # -- the loop ---------------------------------------------------------
+    def serve(self, trace: Sequence[Request]) -> List[Result]:
+        """Replay the trace against the wall clock; one Result per
+        request, ordered by request id."""
+        pending = collections.deque(sorted(trace, key=lambda r: r.arrival))
+        waiting: collections.deque = collections.deque()
+        inflight = []
+        results: Dict[int, Result] = {}
+        admitted_at = {}
+        used = 0.0
+        t0 = time.perf_counter()
+
+        def clock():
+            return time.perf_counter() - t0
+
+        while pending or waiting or inflight:
+            now = clock()
+            while pending and pending[0].arrival <= now:
+                waiting.append(pending.popleft())
+            # admission
+            small, large = [], []
+            blocked = False
+            for req in list(waiting):
+                fits = used + req.footprint <= self.budget or (
+                    used == 0 and not inflight)
+                if fits and not blocked:
+                    waiting.remove(req)
+                    used += req.footprint
+                    self.peak_used = max(self.peak_used, used)
+                    admitted_at[req.rid] = now
+                    if req.num_qubits <= self.small_max and not req.want_grad:
+                        small.append(req)
+                    else:
+                        large.append(req)
+                elif not fits and now - req.arrival > self.reserve_after:
+                    blocked = True  # hold memory for this request
+            by_n = collections.defaultdict(list)
+            for req in small:
+                by_n[req.num_qubits].append(req)
+            for reqs in by_n.values():
+                inflight.extend(self._launch_small(reqs))
+            for req in large:
+                inflight.append(self._launch_large(req))
+            # completion
+            still = []
+            for item in inflight:
+                ev, req, psi, (norms, z0), grads, _keep = item
+                if ev.query():
+                    done = clock()
+                    results[req.rid] = Result(
+                        req.rid, norms.cpu().numpy(), z0.cpu().numpy(),
+                        grads.cpu().numpy() if grads is not None else None,
+                        req.arrival, admitted_at[req.rid], done,
+                        psi if self.keep_states else None)
+                    used -= req.footprint
+                else:
+                    still.append(item)
+            inflight = still
+            if inflight and not waiting:
+                time.sleep(0.0002)
+            elif not inflight and not waiting and pending:
+                time.sleep(max(0.0, min(0.01, pending[0].arrival - clock())))
+        return [results[r.rid] for r in sorted(trace, key=lambda r: r.rid)]
+
+
+def serve_plain(trace: Sequence[Request], device="cuda",
+                keep_states: bool = False) -> List[Result]:
+    """Baseline: FIFO, one request at a time, one kernel per gate."""
+    dev = torch.device(device)
+    out = []
+    t0 = time.perf_counter()
+    for req in sorted(trace, key=lambda r: r.arrival):
+        now = time.perf_counter() - t0
+        if now < req.arrival:
+            time.sleep(req.arrival - now)
+        admitted = time.perf_counter() - t0
+        psi = _init_states(req, dev)
+        grads = None
+        if req.want_grad:
+            grads = _run_grad(req, psi.clone(), fuse=False)
+        # all of the request's gate matrices in one transfer, then one
+        # kernel per gate
+        mats = [torch.from_numpy(g.matrix()) for g in req.gates]
+        by_size = {}
+        for d in (2, 4):
+            sel = [m for m in mats if m.shape[-1] == d]
+            if sel:
+                by_size[d] = iter(torch.stack(sel).to(torch.complex64)
+                                  .pin_memory().to(dev, non_blocking=True))
+        for g, m in zip(req.gates, mats):
+            simulation.apply_operator_(next(by_size[m.shape[-1]]), g.qubits,
+                                       psi)
+        norms, z0 = _outputs(psi, req.num_qubits)
+        res = Result(req.rid, norms.cpu().numpy(), z0.cpu().numpy(),
+                     grads.cpu().numpy() if grads is not None else None,
+                     req.arrival, admitted, time.perf_counter() - t0,
+                     psi if keep_states else None)
+        out.append(res)
+    return sorted(out, key=lambda r: r.rid)
