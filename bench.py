@@ -294,6 +294,33 @@ def bench_adjoint(dev, n=20, layers=12, batch=256, small_batch=8):
             "grad_rel_diff_vs_autograd": agree}
 
 
+# ---------------------------------------------------------------- serving --
+def bench_serving(dev, num=300, rate=150.0, qubits=(10, 22)):
+    """The serving trace (Poisson arrivals; qubits, depth 20-500 and 1-64
+    states uniform; 20% ask for adjoint gradients of <Z_0>; HBM admission
+    budget 160 GB) replayed against the continuous-batching server and the
+    plain per-gate FIFO path.  The qubit range is capped so that both arms
+    finish in seconds (a 28-qubit, 64-state request alone takes minutes on
+    the plain path)."""
+    from qcware_unitair_gb300.serve import (Server, make_trace, serve_plain,
+                                            summarize)
+    warm = make_trace(16, rate=1000.0, seed=99, qubits=qubits,
+                      depth=(20, 100))
+    Server(dev).serve(warm)
+    serve_plain(warm, dev)
+    trace = make_trace(num, rate=rate, seed=0, qubits=qubits)
+    server = summarize(Server(dev).serve(trace))
+    plain = summarize(serve_plain(trace, dev))
+    return {"workload": f"{num} requests, Poisson {rate}/s, qubits "
+                        f"U{{{qubits[0]}..{qubits[1]}}}, depth U{{20..500}}, "
+                        "states U{1..64}, 20% adjoint gradients of <Z_0>, "
+                        "complex64, 160 GB admission budget",
+            "server": server, "plain_per_gate": plain,
+            "throughput_ratio": round(server["circuits_per_s"] /
+                                      plain["circuits_per_s"], 2),
+            "p99_ratio": round(plain["p99_s"] / server["p99_s"], 2)}
+
+
 # -------------------------------------------------------------- GPU arm ---
 def run_gpu(args, ws, rank, local):
     import numpy as np
@@ -474,6 +501,7 @@ def run_gpu(args, ws, rank, local):
     }
     if not args.no_extras:
         result["adjoint"] = bench_adjoint(dev)
+        result["serving"] = bench_serving(dev)
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_sample(n, gates, args.cpu_seconds)
     if rank == 0:

@@ -272,7 +272,21 @@ def _backward_sweep(pc, params, H, psi_L, saved, dtype):
     nbytes = int(L.gbsv_adjoint_scratch_bytes(B, n))
     scratch = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=dev)
     both = buf.view(2 * B, N)
-    segs = pc.segments()
+    # every fixed gate's adjoint, moved to the device in one transfer
+    fixed = [op for op in pc.ops if op[0] == "fixed"]
+    dag = {}
+    if fixed:
+        flat = [op[1].conj().T.contiguous().reshape(-1) for op in fixed]
+        host = torch.cat(flat).to(dtype)
+        if dev.type == "cuda":
+            host = host.pin_memory()
+        devbuf = host.to(dev, non_blocking=True)
+        off = 0
+        for op, f in zip(fixed, flat):
+            d = op[1].shape[-1]
+            dag[id(op)] = devbuf[off:off + f.numel()].view(d, d)
+            off += f.numel()
+    segs = pc.segments() if saved else [(0, len(pc.ops))]
     for si in range(len(segs) - 1, -1, -1):
         a, b = segs[si]
         for op in reversed(pc.ops[a:b]):
@@ -286,7 +300,7 @@ def _backward_sweep(pc, params, H, psi_L, saved, dtype):
                 _lib.check(rc, "adjoint_rotation_step")
             else:
                 _, m, qs, _kind = op
-                md = m.conj().T.contiguous().to(device=dev, dtype=dtype)
+                md = dag[id(op)]
                 rc = L.gbsv_apply_operator(
                     both.data_ptr(), both.data_ptr(), code, n, 2 * B, N,
                     md.data_ptr(), 0, _lib.qubit_array(qs), len(qs), stream)

@@ -37,7 +37,7 @@ import torch
 
 from . import _core, _lib, simulation, states
 from .circuits import Gate, random_circuit, ROTATIONS
-from .fusion import Circuit, FG_DTYPE, _record
+from .fusion import (FG_DTYPE, Program, gate_list_desc, native_plan)
 
 
 @dataclass
@@ -144,14 +144,18 @@ def _grad_circuit(req: Request):
 
 
 def _run_grad(req: Request, psi0: torch.Tensor, fuse: bool = True):
-    from .adjoint import expectation_and_grad
+    """d<Z_0>/d(angle) per state: forward from the gate list (native
+    planner), then the adjoint backward sweep."""
+    from .adjoint import _backward_sweep
     pc, H, angles = _grad_circuit(req)
     dev = psi0.device
     params = torch.tensor(angles or [0.0], dtype=torch.float64)
     params = params.pin_memory().to(dev, non_blocking=True).expand(
         req.num_states, -1).contiguous()
-    _, grads = expectation_and_grad(pc, params, H, psi0=psi0, fuse=fuse)
-    return grads
+    psi = psi0.clone()
+    Program.from_gate_list(req.gates, req.num_qubits, torch.complex64, dev,
+                           fuse=fuse).run(psi, inplace=True)
+    return _backward_sweep(pc, params, H, psi, [], torch.complex64)
 
 
 # ----------------------------------------------------------------- server --
@@ -184,28 +188,31 @@ class Server:
             items = [(req, _init_states(req, self.device)) for req in reqs]
         recs, pool_parts, first, count, ptrs = [], [], [], [], []
         pool_len = 0
-        local = {p: p for p in range(n)}
+        nrec = 0
         for req, psi in items:
-            f0 = len(recs)
-            for g in Circuit.from_gates(n, req.gates).gates:
-                rec, vals = _record(g, n, local, None)
-                v = vals.reshape(-1).to(torch.complex64)
-                rec["mat"], rec["mat_bstride"] = pool_len, 0
-                pool_parts.append(v)
-                pool_len += v.numel()
-                recs.append(rec)
+            # one whole-state stage per request, planned natively
+            desc, mats = gate_list_desc(req.gates)
+            nat = native_plan(None, n, n, n, 0, True, torch.complex64,
+                              desc, mats)
+            r = nat["records"].copy()
+            r["mat"] += pool_len
+            recs.append(r)
+            pool_parts.append(nat["pool"])
+            pool_len += len(nat["pool"])
+            f0 = nrec
+            nrec += len(r)
             N = 2 ** n
             base = psi.data_ptr()
             for j in range(req.num_states):
                 ptrs.append(base + j * N * 8)
                 first.append(f0)
-                count.append(len(recs) - f0)
+                count.append(nrec - f0)
         dev = self.device
         with torch.cuda.stream(stream):
-            gates = torch.from_numpy(np.stack(recs).view(np.uint8).copy()) \
-                if recs else torch.zeros(48, dtype=torch.uint8)
-            pool = torch.cat(pool_parts) if pool_parts else \
-                torch.zeros(1, dtype=torch.complex64)
+            allr = np.concatenate(recs) if recs else np.zeros(1, FG_DTYPE)
+            gates = torch.from_numpy(allr.view(np.uint8).copy())
+            pool = torch.from_numpy(np.concatenate(pool_parts)) \
+                if pool_len else torch.zeros(1, dtype=torch.complex64)
             gates = gates.pin_memory().to(dev, non_blocking=True)
             pool = pool.pin_memory().to(dev, non_blocking=True)
             meta = torch.tensor(ptrs, dtype=torch.int64).pin_memory().to(
@@ -232,8 +239,8 @@ class Server:
             grads = None
             if req.want_grad:
                 grads = _run_grad(req, psi.clone())
-            prog = Circuit.from_gates(req.num_qubits, req.gates).compile(
-                torch.complex64, self.device)
+            prog = Program.from_gate_list(req.gates, req.num_qubits,
+                                          torch.complex64, self.device)
             prog.run(psi, inplace=True)
             o = _outputs(psi, req.num_qubits)
             ev = torch.cuda.Event()
