@@ -188,6 +188,43 @@ int gbsv_run_programs(int dtype, int num_qubits, int num_ctas,
                       const void* gate_count, const void* gates,
                       const void* pool, void* stream);
 
+/* ---- permutations, multi-controlled gates, sampling -------------------- */
+
+/* out qubit j <- in qubit perm[j] (perm a HOST array of num_qubits entries;
+ * out != in).  Replaces unitair's permute_qubits / swap / roll_qubits
+ * (src/unitair/simulation/operations.py:506-654). */
+int gbsv_permute_qubits(const void* in, void* out, int dtype, int num_qubits,
+                        int64_t num_states, const int32_t* perm,
+                        void* stream);
+
+/* out = (-1)^k * in where k counts the masks (device array of uint64
+ * amplitude-index bit masks, at most 256) whose bits are all set in the
+ * amplitude index; in place allowed.  One mask per (control, target) pair
+ * is unitair's multi_cz (operations.py:657-748); one mask over all listed
+ * qubits is multi_controlled_z (:751-783). */
+int gbsv_phase_flip(const void* in, void* out, int dtype, int num_qubits,
+                    int64_t num_states, const void* masks, int num_masks,
+                    void* stream);
+
+/* X on `target` where every control qubit (HOST array) is 1; in place
+ * allowed.  unitair's multi_controlled_x (operations.py:786-805) builds it
+ * as H, multi_controlled_z, H. */
+int gbsv_multi_controlled_x(const void* in, void* out, int dtype,
+                            int num_qubits, int64_t num_states,
+                            const int32_t* controls, int num_controls,
+                            int target, void* stream);
+
+/* Scratch bytes gbsv_sample needs for a state of `dim` amplitudes. */
+size_t gbsv_sample_scratch_bytes(int64_t dim);
+
+/* Draw num_samples basis indices from |state|^2 / sum |state|^2 (one state
+ * of dim = 2^n amplitudes) into out_indices (device int64).  Samples are a
+ * pure function of (seed, sample number).  Replaces the sampling in
+ * unitair's measure (src/unitair/simulation/measurement.py:9-70). */
+int gbsv_sample(const void* state, int dtype, int64_t dim,
+                int64_t num_samples, uint64_t seed, int64_t* out_indices,
+                void* scratch, size_t scratch_bytes, void* stream);
+
 /* ---- host-side circuit planner ------------------------------------------ */
 
 /* One gate of a circuit to plan (host memory).  kind: 0 dense, 1 diagonal,

@@ -11,7 +11,12 @@ from .states import (StateLayout, StateShapeError, count_qubits,  # noqa
                      hilbert_space_dim, diag_expectation_value,
                      inner_product, norm_squared, abs_squared)
 from .simulation import (apply_operator, apply_operator_, apply_all_qubits,  # noqa
-                         apply_each_qubit, apply_phase, act_first_qubits)
+                         apply_each_qubit, apply_phase, act_first_qubits,
+                         apply_to_qubits, act_last_qubit, swap,
+                         permute_qubits, roll_qubits, multi_cz,
+                         multi_controlled_z, multi_controlled_x)
+from .measurement import measure, MeasurementHistogram  # noqa
+from .fusion import Circuit, Program  # noqa
 from .initializations import (unit_vector, uniform_superposition,  # noqa
                               rand_state)
 

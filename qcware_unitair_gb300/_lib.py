@@ -95,6 +95,14 @@ SIGNATURES = {
     "gbsv_adjoint_rotation_step": (_I, [_P, _P, _I, _I, _I64, _I, _I, _P, _I,
                                         _I64, ctypes.c_double, _P, _I64,
                                         ctypes.c_double, _P, _SZ, _P]),
+    "gbsv_permute_qubits": (_I, [_P, _P, _I, _I, _I64,
+                                 ctypes.POINTER(_I32), _P]),
+    "gbsv_phase_flip": (_I, [_P, _P, _I, _I, _I64, _P, _I, _P]),
+    "gbsv_multi_controlled_x": (_I, [_P, _P, _I, _I, _I64,
+                                     ctypes.POINTER(_I32), _I, _I, _P]),
+    "gbsv_sample_scratch_bytes": (_SZ, [_I64]),
+    "gbsv_sample": (_I, [_P, _I, _I64, _I64, ctypes.c_uint64, _P, _P, _SZ,
+                         _P]),
     "gbsv_reduce_scratch_bytes": (_SZ, [_I64, _I64]),
     "gbsv_norm_squared": (_I, [_P, _I, _I64, _I64, _P, _I, _P, _SZ, _P]),
     "gbsv_norm_squared_noalloc": (_I, [_P, _I, _I64, _I64, _P, _I, _P]),

@@ -384,3 +384,198 @@ def apply_phase(angles: torch.Tensor, state: torch.Tensor) -> torch.Tensor:
     broadcasting (operations.py:15-42).  float64 angles on a complex64
     state give a complex128 result, as in unitair."""
     return _ApplyPhase.apply(angles, state)
+
+
+# ------------------------------------------------ permutations and friends --
+def _permute(state: torch.Tensor, perm, n: int) -> torch.Tensor:
+    _core.require_cuda(state)
+    code = _core.complex_code(state.dtype)
+    s = state.contiguous()
+    out = torch.empty_like(s)
+    if s.numel():
+        rc = _lib.load().gbsv_permute_qubits(
+            s.data_ptr(), out.data_ptr(), code, n, s.numel() >> n,
+            _lib.qubit_array(perm), _core.stream_of(s.device))
+        _lib.check(rc, "permute_qubits")
+    return out
+
+
+def permute_qubits(permutation: Iterable[int],
+                   state_vector: torch.Tensor) -> torch.Tensor:
+    """Output qubit j is input qubit permutation[j], batch dims untouched
+    (operations.py:600-654)."""
+    n = count_qubits(state_vector)
+    perm = [int(p) for p in permutation]
+    if sorted(perm) != list(range(n)):
+        raise RuntimeError(f"permute(): {perm} is not a permutation of the "
+                           f"{n} qubit dims")
+    return _permute(state_vector, perm, n)
+
+
+def swap(state: torch.Tensor, qubit_pair: Tuple[int, int]) -> torch.Tensor:
+    """Exchange two qubits (operations.py:506-537); negative indices count
+    from the last qubit, as in get_qubit_indices."""
+    n = count_qubits(state)
+    if qubit_pair[0] == qubit_pair[1]:
+        return state
+    qs = []
+    for q in qubit_pair:
+        q = int(q)
+        if q >= n or q < -n:
+            raise ValueError(
+                "Expected index in {-num_qubits, ..., num_qubits - 1}.\n"
+                f"Num_qubits: {n}, index: {list(qubit_pair)}.")
+        qs.append(q % n)
+    if qs[0] == qs[1]:
+        return state
+    perm = list(range(n))
+    perm[qs[0]], perm[qs[1]] = qs[1], qs[0]
+    return _permute(state, perm, n)
+
+
+def roll_qubits(state: torch.Tensor, num_steps: int = 1) -> torch.Tensor:
+    """Cyclic qubit shift: out[a_0..a_{n-1}] = in[a_k, ..., a_{k-1}] with
+    k = num_steps mod n (operations.py:540-597)."""
+    n = count_qubits(state)
+    k = num_steps % n if n else 0
+    if k == 0:
+        return state
+    perm = [(j - k) % n for j in range(n)]
+    return _permute(state, perm, n)
+
+
+def act_last_qubit(single_qubit_operator: torch.Tensor,
+                   state: torch.Tensor) -> torch.Tensor:
+    """Deprecated in unitair (operations.py:189-213): the operator on the
+    last qubit."""
+    import warnings
+    warnings.warn(
+        "act_last_qubit and act_last_qubit_tensor are outdated. These\n"
+        "functions will be removed from Unitair in a later release or may\n"
+        "be revised to meet our current standards.\n"
+        "Please consider using apply_operator instead.")
+    n = count_qubits(state)
+    return apply_operator(single_qubit_operator, [n - 1], state)
+
+
+def apply_to_qubits(operators: Iterable[torch.Tensor], qubits: Iterable[int],
+                    state: torch.Tensor) -> torch.Tensor:
+    """Single-qubit operators on the listed qubits in order
+    (operations.py:416-503).  Operators on the same qubit are multiplied
+    first, as unitair does (gates/matrix_algebra.py:6-51); with unbatched
+    operators the fused per-qubit gates then run as one fused program."""
+    n = count_qubits(state)
+    fused: dict = {}
+    for q, op in zip(qubits, operators):
+        q = int(q)
+        if not 0 <= q < n:
+            raise ValueError(
+                "Expected index in {-num_qubits, ..., num_qubits - 1}.\n"
+                f"Num_qubits: {n}, index: {q}.")
+        fused[q] = torch.matmul(op, fused[q]) if q in fused else op
+    if not fused:
+        return state.contiguous()
+    ops = list(fused.items())
+    _core.require_cuda(state, *[op for _, op in ops])
+    grad = torch.is_grad_enabled() and (
+        state.requires_grad or any(op.requires_grad for _, op in ops))
+    if grad or any(op.dim() != 2 for _, op in ops):
+        out = state
+        for q, op in ops:
+            out = apply_operator(op, [q], out)
+        return out
+    for _, op in ops:
+        _check_dtypes(op, state)
+    from .fusion import Circuit
+    circ = Circuit(n)
+    for q, op in ops:
+        circ.append(op, [q], "dense")
+    prog = circ.compile(state.dtype, state.device)
+    return prog.run(state.contiguous())
+
+
+def _mask_of(qubits, n):
+    m = 0
+    for q in qubits:
+        m |= 1 << (n - 1 - int(q))
+    return m
+
+
+def _phase_flip(state: torch.Tensor, masks) -> torch.Tensor:
+    n = count_qubits(state)
+    _core.require_cuda(state)
+    code = _core.complex_code(state.dtype)
+    s = state.contiguous()
+    out = torch.empty_like(s)
+    if s.numel() == 0:
+        return out
+    host = torch.tensor([int(m) for m in masks] or [0], dtype=torch.int64)
+    dev_masks = host.pin_memory().to(s.device, non_blocking=True)
+    rc = _lib.load().gbsv_phase_flip(
+        s.data_ptr(), out.data_ptr(), code, n, s.numel() >> n,
+        dev_masks.data_ptr(), len(masks), _core.stream_of(s.device))
+    _lib.check(rc, "phase_flip")
+    return out
+
+
+def multi_cz(qubit_pairs: torch.Tensor, state_vector: torch.Tensor,
+             num_bits_memory_cutoff: Optional[int] = None) -> torch.Tensor:
+    """CZ on each (control, target) row of ``qubit_pairs`` (shape (2,) or
+    (num_pairs, 2)) in one pass (operations.py:657-748).
+    ``num_bits_memory_cutoff`` only tuned unitair's temporaries and is
+    accepted for compatibility."""
+    n = count_qubits(state_vector)
+    if qubit_pairs.dim() == 1:
+        qubit_pairs = qubit_pairs.view(1, 2)
+    if state_vector.device.type != qubit_pairs.device.type:
+        raise ValueError(
+            "state_vector and qubit_qubit_pairs must have same device.")
+    elif qubit_pairs.dim() != 2:
+        raise ValueError("qubit_pairs must have size (2,) or (num_pairs, 2).")
+    pairs = qubit_pairs.cpu().tolist()
+    if any(q >= n for row in pairs for q in row):
+        raise ValueError(
+            "Control/target indices for CZ gate must be less than num_bits.")
+    if any(q < 0 for row in pairs for q in row):
+        raise ValueError("Control/target indices must be non-negative.")
+    if any(row[0] == row[1] for row in pairs):
+        raise ValueError("Control and target qubits are not distinct.")
+    return _phase_flip(state_vector, [_mask_of(r, n) for r in pairs])
+
+
+def multi_controlled_z(qubits: Iterable[int],
+                       state_vector: torch.Tensor) -> torch.Tensor:
+    """C..CZ on ``qubits``: -1 where all of them are 1
+    (operations.py:751-783; unlike unitair, works on CUDA tensors)."""
+    n = count_qubits(state_vector)
+    qubits = [int(q) for q in qubits]
+    if len(set(qubits)) != len(qubits) or any(
+            q < 0 or q >= n for q in qubits):
+        raise ValueError(f"qubits={qubits} are not distinct qubits of a "
+                         f"{n}-qubit state.")
+    return _phase_flip(state_vector, [_mask_of(qubits, n)])
+
+
+def multi_controlled_x(state_vector: torch.Tensor, controls: Iterable[int],
+                       target: int) -> torch.Tensor:
+    """X on ``target`` where every control is 1 (operations.py:786-805),
+    as one exact swap pass instead of H, C..CZ, H."""
+    n = count_qubits(state_vector)
+    controls = [int(c) for c in controls]
+    target = int(target)
+    if target < 0 or target >= n or target in controls or len(
+            set(controls)) != len(controls) or any(
+                c < 0 or c >= n for c in controls):
+        raise ValueError(f"bad controls {controls} / target {target} for "
+                         f"{n} qubits")
+    _core.require_cuda(state_vector)
+    code = _core.complex_code(state_vector.dtype)
+    s = state_vector.contiguous()
+    out = torch.empty_like(s)
+    if s.numel():
+        rc = _lib.load().gbsv_multi_controlled_x(
+            s.data_ptr(), out.data_ptr(), code, n, s.numel() >> n,
+            _lib.qubit_array(controls), len(controls), target,
+            _core.stream_of(s.device))
+        _lib.check(rc, "multi_controlled_x")
+    return out

@@ -205,6 +205,40 @@ def main(ref_root: str) -> None:
         put(name, op=op, state=st, w=w, out=out, gop=op.grad, gstate=st.grad)
         cases.append({"name": name, "kind": "grad", "qubits": qs, "n": n})
 
+    # ---- permutations, apply_to_qubits, multi-controlled gates ----------
+    from unitair.simulation.operations import (
+        swap, permute_qubits, roll_qubits, apply_to_qubits, multi_cz,
+        multi_controlled_z, multi_controlled_x)
+    for j, (dtype, shape) in enumerate([(torch.complex64, (3, 2 ** 6)),
+                                        (torch.complex128, (2 ** 5,))]):
+        st = cplx(shape, dtype)
+        n = 6 if len(shape) == 2 else 5
+        name = f"perm_{j}"
+        put(name, state=st,
+            swap=swap(st, (1, n - 1)), swap_neg=swap(st, (0, -1)),
+            perm=permute_qubits(list(reversed(range(n))), st),
+            perm2=permute_qubits([2, 0, 1] + list(range(3, n)), st),
+            roll1=roll_qubits(st, 1), roll3=roll_qubits(st, 3),
+            rollm=roll_qubits(st, -2))
+        cases.append({"name": name, "kind": "perm", "n": n})
+    for j, (dtype, ob) in enumerate([(torch.complex64, ()),
+                                     (torch.complex128, ())]):
+        n = 5
+        st = cplx((3, 2 ** n), dtype)
+        qs = [0, 3, 0, 4, 1, 3]
+        ops = [cplx(ob + (2, 2), dtype) for _ in qs]
+        name = f"tq_{j}"
+        put(name, state=st, ops=torch.stack(ops),
+            out=apply_to_qubits(ops, qs, st))
+        cases.append({"name": name, "kind": "to_qubits", "qubits": qs})
+    st = cplx((2, 2 ** 6), torch.complex64)
+    pairs = torch.tensor([[0, 1], [2, 5], [1, 4], [0, 1]])
+    put("mcz_0", state=st, pairs=pairs, out=multi_cz(pairs, st),
+        single=multi_cz(torch.tensor([3, 1]), st),
+        mcz=multi_controlled_z([1, 4, 2], st),
+        mcx=multi_controlled_x(st, [0, 5], 2))
+    cases.append({"name": "mcz_0", "kind": "multi"})
+
     # ---- variational gradient through unitair + torch autograd -----------
     # ansatz: per layer, on every qubit RZ(phi) then RY(theta) (U = RY RZ),
     # then a CZ ring; loss = mean_b <sum_i Z_i + 0.5 sum_i X_i X_{i+1}>.
