@@ -1,0 +1,109 @@
+"""apply_to_qubits, swap / permute_qubits / roll_qubits, multi_cz,
+multi_controlled_z / x and measure against the reference's outputs
+(golden vectors) and, for sampling, against |psi|^2."""
+import numpy as np
+import pytest
+import torch
+
+import qcware_unitair_gb300 as ug
+from conftest import golden_data
+
+pytestmark = pytest.mark.gpu
+G = golden_data()
+DEV = torch.device("cuda:0")
+
+
+def cu(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(DEV)
+
+
+def close(got, ref, tol):
+    got = got.cpu().numpy()
+    assert got.shape == ref.shape
+    assert np.abs(got - ref).max() <= tol * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.parametrize("case", G.of_kind("perm"), ids=lambda c: c["name"])
+def test_permutations_exact(case):
+    st = cu(G[case["name"] + "/state"])
+    n = case["n"]
+    g = lambda k: G[case["name"] + "/" + k]
+    # pure permutations: bit-exact
+    assert np.array_equal(ug.swap(st, (1, n - 1)).cpu().numpy(), g("swap"))
+    assert np.array_equal(ug.swap(st, (0, -1)).cpu().numpy(), g("swap_neg"))
+    assert np.array_equal(ug.permute_qubits(list(reversed(range(n))),
+                                            st).cpu().numpy(), g("perm"))
+    assert np.array_equal(ug.permute_qubits([2, 0, 1] + list(range(3, n)),
+                                            st).cpu().numpy(), g("perm2"))
+    assert np.array_equal(ug.roll_qubits(st, 1).cpu().numpy(), g("roll1"))
+    assert np.array_equal(ug.roll_qubits(st, 3).cpu().numpy(), g("roll3"))
+    assert np.array_equal(ug.roll_qubits(st, -2).cpu().numpy(), g("rollm"))
+    assert ug.swap(st, (2, 2)) is st
+
+
+@pytest.mark.parametrize("case", G.of_kind("to_qubits"),
+                         ids=lambda c: c["name"])
+def test_apply_to_qubits(case):
+    st = cu(G[case["name"] + "/state"])
+    ops = cu(G[case["name"] + "/ops"])
+    ref = G[case["name"] + "/out"]
+    tol = 1e-5 if ref.dtype == np.complex64 else 1e-12
+    got = ug.apply_to_qubits(list(ops), case["qubits"], st)
+    close(got, ref, 8 * tol)
+
+
+def test_multi_controlled():
+    st = cu(G["mcz_0/state"])
+    pairs = torch.from_numpy(G["mcz_0/pairs"]).to(DEV)
+    assert np.array_equal(ug.multi_cz(pairs, st).cpu().numpy(),
+                          G["mcz_0/out"])
+    assert np.array_equal(
+        ug.multi_cz(torch.tensor([3, 1], device=DEV), st).cpu().numpy(),
+        G["mcz_0/single"])
+    assert np.array_equal(ug.multi_controlled_z([1, 4, 2], st).cpu().numpy(),
+                          G["mcz_0/mcz"])
+    # unitair builds it as H, C..CZ, H: equal up to that rounding
+    close(ug.multi_controlled_x(st, [0, 5], 2), G["mcz_0/mcx"], 1e-6)
+    with pytest.raises(ValueError):
+        ug.multi_cz(torch.tensor([[0, 0]], device=DEV), st)
+    with pytest.raises(ValueError):
+        ug.multi_cz(torch.tensor([0, 1]), st)  # device mismatch
+
+
+def test_measure_distribution():
+    n = 10
+    rng = np.random.default_rng(0)
+    amps = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+    amps[::7] = 0  # zero-probability outcomes must never be drawn
+    amps /= np.linalg.norm(amps)
+    st = cu(amps.astype(np.complex64))
+    N = 400000
+    idx = ug.measurement.sample(st, N, seed=123).cpu().numpy()
+    assert idx.min() >= 0 and idx.max() < 2 ** n
+    assert not np.any(np.isin(idx, np.arange(0, 2 ** n, 7)))
+    freq = np.bincount(idx, minlength=2 ** n) / N
+    p = np.abs(amps) ** 2
+    # each bin within 6 sigma of its binomial mean
+    sigma = np.sqrt(p * (1 - p) / N) + 1e-12
+    assert np.all(np.abs(freq - p) <= 6 * sigma + 1e-9)
+    again = ug.measurement.sample(st, N, seed=123).cpu().numpy()
+    assert np.array_equal(idx, again)  # a function of the seed only
+    h = ug.measure(st, 1000, seed=5)
+    assert sum(h.histogram.values()) == 1000
+    counts = list(h.histogram.values())
+    assert counts == sorted(counts, reverse=True)
+    assert all(len(k) == n for k in h.histogram)
+    raw = ug.measure(st, 1000, raw_output=True, seed=5)
+    assert sum(raw.values()) == 1000
+    assert h["0" * n] == raw.get(0, 0)
+
+
+def test_measure_large_state_chunks():
+    n = 22
+    st = torch.zeros(2 ** n, dtype=torch.complex64, device=DEV)
+    st[5] = 0.6
+    st[2 ** n - 3] = 0.8j
+    idx = ug.measurement.sample(st, 100000, seed=1).cpu().numpy()
+    assert set(np.unique(idx)) == {5, 2 ** n - 3}
+    frac = np.mean(idx == 5)
+    assert abs(frac - 0.36) < 0.01
