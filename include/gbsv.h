@@ -338,6 +338,36 @@ int gbsv_adjoint_rotation_step(void* psi, void* lam, int dtype,
                                void* scratch, size_t scratch_bytes,
                                void* stream);
 
+/* One op of a fused backward stage (80 bytes, device memory): kind 0 is a
+ * rotation exp(-i theta/2 P) (gen 0 X, 1 Y, 2 Z) on tile bit `bit` (or
+ * -1 - position outside the tile, Z only) with theta = scale *
+ * params[s * num_params + pidx] whose gradient goes to `slot`; kind 1 is a
+ * fixed gate whose ADJOINT is the record g (kinds 0-2 of
+ * gbsv_fused_gate_t, values in pool). */
+typedef struct gbsv_adjoint_op {
+  int32_t kind, gen, bit, slot, pidx, pad_;
+  double scale;
+  gbsv_fused_gate_t g;
+} gbsv_adjoint_op_t;
+
+/* One fused backward stage of the adjoint method over the tiles of psi and
+ * lam (same tile rules as gbsv_run_stage; tile_positions on the host):
+ * applies the ops in order to both states in shared memory, one read and
+ * one write of each state, and for every rotation adds
+ *   slot_scale[k] * Im <lam_s|P|psi_s>   (FP64, summed over the state's
+ * tiles in index order) to grad[s * num_params + slot_param[k]].
+ * slot_param / slot_scale are device arrays of num_slots entries; scratch
+ * holds num_slots * num_states * 2^(n - tile_qubits) doubles. */
+int gbsv_adjoint_stage(void* psi, void* lam, int dtype, int num_qubits,
+                       int64_t num_states, int tile_qubits,
+                       int contiguous_qubits, const int32_t* tile_positions,
+                       const void* ops, int num_ops, const void* pool,
+                       const void* params, int params_dtype,
+                       int64_t num_params, int num_slots,
+                       const int32_t* slot_param, const double* slot_scale,
+                       double* grad, void* scratch, size_t scratch_bytes,
+                       void* stream);
+
 /* ---- reductions (FP64 accumulation) ----------------------------------- */
 
 /* Scratch bytes a reduction over num_rows rows of length dim needs; 0 means

@@ -103,6 +103,9 @@ SIGNATURES = {
     "gbsv_sample_scratch_bytes": (_SZ, [_I64]),
     "gbsv_sample": (_I, [_P, _I, _I64, _I64, ctypes.c_uint64, _P, _P, _SZ,
                          _P]),
+    "gbsv_adjoint_stage": (_I, [_P, _P, _I, _I, _I64, _I, _I,
+                                ctypes.POINTER(_I32), _P, _I, _P, _P, _I,
+                                _I64, _I, _P, _P, _P, _P, _SZ, _P]),
     "gbsv_reduce_scratch_bytes": (_SZ, [_I64, _I64]),
     "gbsv_norm_squared": (_I, [_P, _I, _I64, _I64, _P, _I, _P, _SZ, _P]),
     "gbsv_norm_squared_noalloc": (_I, [_P, _I, _I64, _I64, _P, _I, _P]),

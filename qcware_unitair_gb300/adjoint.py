@@ -29,7 +29,11 @@ from typing import Dict, List, Optional, Sequence
 import numpy as np
 import torch
 
+import ctypes
+
 from . import _core, _lib, states
+
+ctypes_int32 = ctypes.c_int32
 from .circuits import gate_matrix
 from .fusion import CTRL, DENSE, DIAG, Circuit
 
@@ -319,6 +323,153 @@ def evaluate(pc: ParamCircuit, params: torch.Tensor, H: PauliSum,
     return pauli_expectation(H, psi_L)
 
 
+ADJOP_DTYPE = np.dtype([("kind", "<i4"), ("gen", "<i4"), ("bit", "<i4"),
+                        ("slot", "<i4"), ("pidx", "<i4"), ("pad", "<i4"),
+                        ("scale", "<f8")])
+
+
+def _adjop_dtype():
+    from .fusion import FG_DTYPE
+    return np.dtype(ADJOP_DTYPE.descr + [("g", FG_DTYPE)])
+
+
+def _plan_backward(pc: ParamCircuit, a: int, b: int, dtype, dev, m: int):
+    """Fused backward stages for ops [a, b) walked in reverse: a list of
+    ("stage", launch args) / ("rot", op) / ("fixed", op) entries.  Depends
+    only on the circuit's structure, so it is cached per circuit."""
+    from .fusion import CircuitGate, FG_DTYPE, _record, _to_device, plan
+    n = pc.num_qubits
+    ops = list(reversed(pc.ops[a:b]))
+    stand = []
+    dummy = torch.zeros(2, 2, dtype=torch.complex128)
+    for op in ops:
+        if op[0] == "rot":
+            stand.append(CircuitGate(dummy, (op[2],),
+                                     DIAG if op[1] == "Z" else DENSE))
+        else:
+            _, mat, qs, kind = op
+            stand.append(CircuitGate(mat.conj().transpose(-1, -2), qs,
+                                     kind or DENSE))
+    index = {id(g): op for g, op in zip(stand, ops)}
+    c_min = min(4 if dtype == torch.complex64 else 3, m)
+    out = []
+    AD = _adjop_dtype()
+    for kind, item in plan(stand, n, m, c_min):
+        if kind == "plain":
+            op = index[id(item)]
+            out.append(("rot" if op[0] == "rot" else "fixed", op))
+            continue
+        tile = item.tile
+        c = 0
+        while c in tile:
+            c += 1
+        c = min(c, m)
+        order = list(range(c)) + sorted(p for p in tile if p >= c)
+        local = {p: i for i, p in enumerate(order)}
+        recs, pool, slot_p, slot_s = [], [], [], []
+        pool_len = 0
+        for g in item.gates:
+            op = index[id(g)]
+            r = np.zeros((), dtype=AD)
+            if op[0] == "rot":
+                _, gen, q, pi, scale = op
+                pos = n - 1 - q
+                r["kind"], r["gen"] = 0, GEN[gen]
+                r["bit"] = local[pos] if pos in local else -1 - pos
+                r["slot"], r["pidx"], r["scale"] = len(slot_p), pi, scale
+                slot_p.append(pi)
+                slot_s.append(scale)
+            else:
+                rec, vals = _record(g, n, local, None)
+                v = vals.reshape(-1).to(dtype)
+                rec["mat"], rec["mat_bstride"] = pool_len, 0
+                pool.append(v)
+                pool_len += v.numel()
+                r["kind"] = 1
+                r["g"] = rec
+            recs.append(r)
+        args = {
+            "c": c, "positions": (ctypes_int32 * m)(*order),
+            "ops": _to_device(np.stack(recs).view(np.uint8), dev),
+            "num_ops": len(recs),
+            "pool": (torch.cat(pool) if pool else torch.zeros(1, dtype=dtype)
+                     ).to(dev),
+            "num_slots": len(slot_p),
+            "slot_param": torch.tensor(slot_p or [0], dtype=torch.int32,
+                                       device=dev),
+            "slot_scale": torch.tensor(slot_s or [0.0], dtype=torch.float64,
+                                       device=dev)}
+        out.append(("stage", args))
+    return out
+
+
+def _backward_fused(pc, params, H, psi_L, saved, dtype):
+    """The adjoint sweep with fused backward stages (see the kernel
+    gbsv_adjoint_stage): one read and write of psi and lambda per stage."""
+    n, B = pc.num_qubits, params.shape[0]
+    dev = params.device
+    N = 2 ** n
+    m = min(12 if dtype == torch.complex64 else 11, n)
+    buf = torch.empty(2, B, N, dtype=dtype, device=dev)
+    psi, lam = buf[0], buf[1]
+    psi.copy_(psi_L)
+    _pauli_apply(H, psi, lam)
+    grads = torch.zeros(B, pc.num_params, dtype=torch.float64, device=dev)
+    p = params.detach().contiguous()
+    if p.dtype not in (torch.float32, torch.float64):
+        p = p.to(torch.float64)
+    L = _lib.load()
+    code = _core.complex_code(dtype)
+    pcode = _core.real_code(p.dtype)
+    stream = _core.stream_of(dev)
+    segs = pc.segments() if saved else [(0, len(pc.ops))]
+    cache = pc.__dict__.setdefault("_adj_cache", {})
+    tiles = B << (n - m)
+    scratch = None
+    both = buf.view(2 * B, N)
+    for si in range(len(segs) - 1, -1, -1):
+        a, b = segs[si]
+        key = (a, b, dtype, str(dev), m)
+        if key not in cache:
+            cache[key] = _plan_backward(pc, a, b, dtype, dev, m)
+        for entry in cache[key]:
+            if entry[0] == "stage":
+                st = entry[1]
+                need = st["num_slots"] * tiles * 8
+                if need and (scratch is None or scratch.numel() < need):
+                    scratch = torch.empty(need, dtype=torch.uint8, device=dev)
+                rc = L.gbsv_adjoint_stage(
+                    psi.data_ptr(), lam.data_ptr(), code, n, B, m, st["c"],
+                    st["positions"], st["ops"].data_ptr(), st["num_ops"],
+                    st["pool"].data_ptr(), p.data_ptr(), pcode,
+                    pc.num_params, st["num_slots"],
+                    st["slot_param"].data_ptr(), st["slot_scale"].data_ptr(),
+                    grads.data_ptr(),
+                    scratch.data_ptr() if need else None, need, stream)
+                _lib.check(rc, "adjoint_stage")
+            elif entry[0] == "rot":
+                _, gen, q, pi, scale = entry[1]
+                nbytes = int(L.gbsv_adjoint_scratch_bytes(B, n))
+                sc = torch.empty(max(nbytes, 16), dtype=torch.uint8,
+                                 device=dev)
+                rc = L.gbsv_adjoint_rotation_step(
+                    psi.data_ptr(), lam.data_ptr(), code, n, B, q, GEN[gen],
+                    p.data_ptr() + pi * p.element_size(), pcode,
+                    pc.num_params, scale, grads.data_ptr() + pi * 8,
+                    pc.num_params, scale, sc.data_ptr(), nbytes, stream)
+                _lib.check(rc, "adjoint_rotation_step")
+            else:
+                _, m_, qs, _k = entry[1]
+                md = m_.conj().T.contiguous().to(device=dev, dtype=dtype)
+                rc = L.gbsv_apply_operator(
+                    both.data_ptr(), both.data_ptr(), code, n, 2 * B, N,
+                    md.data_ptr(), 0, _lib.qubit_array(qs), len(qs), stream)
+                _lib.check(rc, "apply_operator")
+        if saved:
+            psi.copy_(saved[si])
+    return grads
+
+
 def expectation_and_grad(pc: ParamCircuit, params: torch.Tensor,
                          H: PauliSum, psi0: Optional[torch.Tensor] = None,
                          dtype=torch.complex64, checkpoints: bool = True,
@@ -328,7 +479,8 @@ def expectation_and_grad(pc: ParamCircuit, params: torch.Tensor,
     _core.require_cuda(params)
     psi_L, saved = _forward(pc, params, dtype, psi0, checkpoints, fuse)
     values = pauli_expectation(H, psi_L)
-    grads = _backward_sweep(pc, params, H, psi_L, saved, dtype)
+    sweep = _backward_fused if fuse else _backward_sweep
+    grads = sweep(pc, params, H, psi_L, saved, dtype)
     return values, grads
 
 
@@ -344,8 +496,8 @@ class _Expectation(torch.autograd.Function):
     @staticmethod
     def backward(ctx, g):
         (params,) = ctx.saved_tensors
-        grads = _backward_sweep(ctx.pc, params, ctx.H, ctx.psi_L, ctx.saved,
-                                ctx.dtype)
+        grads = _backward_fused(ctx.pc, params, ctx.H, ctx.psi_L,
+                                ctx.saved, ctx.dtype)
         ctx.psi_L = ctx.saved = None
         out = (g.to(torch.float64).unsqueeze(-1) * grads).to(params.dtype)
         return out, None, None, None, None, None

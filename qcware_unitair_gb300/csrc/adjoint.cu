@@ -265,3 +265,393 @@ extern "C" int gbsv_adjoint_rotation_step(
                                        grad_stride, grad_factor);
   return after_launch("adjoint_finalize");
 }
+
+// ---------------------------------------------------------------------------
+// Fused backward stages: one read and one write of psi and lambda per stage
+// instead of per gate.  A stage holds the tiles of both states (same tile
+// bits as a forward stage) in shared memory and walks its ops (the circuit's
+// gates in reverse):
+//   rotation U = exp(-i theta/2 P) on tile bit b (P = Z may also sit on a
+//     bit outside the tile): accumulates Im <lambda|P|psi> over the tile,
+//     block-reduces it into partial[slot][tile], and applies U^dag to both
+//     tiles in the same sweep;
+//   fixed gate: its adjoint (a gate record as in the forward stages, with
+//     the conjugate-transposed matrix) is applied to both tiles; diagonal
+//     factors from bits outside the tile multiply both states equally, so
+//     they are deferred to the store and leave <lambda|P|psi> unchanged.
+// A second kernel sums the partials of each (rotation, state) over the
+// state's tiles in index order and adds them to the gradient.
+namespace gbsv {
+
+struct AdjOp {
+  int32_t kind;   // 0 rotation, 1 fixed gate
+  int32_t gen;    // rotation generator: 0 X, 1 Y, 2 Z
+  int32_t bit;    // rotation: tile bit, or -1 - position (Z only)
+  int32_t slot;   // rotation: gradient slot in this stage
+  int32_t pidx;   // rotation: parameter index
+  int32_t pad_;
+  double scale;   // rotation: theta = scale * params[s, pidx]
+  FusedGate g;    // fixed gate: record of its adjoint
+};
+
+struct AdjStageArgs {
+  int n, m, c;
+  int hpos[14];
+  int spos[14];
+  const AdjOp* ops;
+  int num_ops;
+  const void* params;
+  int params_f64;
+  int64_t num_params;
+};
+
+__device__ __forceinline__ int aswz(int l) {
+  const int u = l >> 1;
+  return ((u ^ ((u >> 3) & 7)) << 1) | (l & 1);
+}
+
+template <typename R>
+__device__ __forceinline__ void adj_fixed(Cx<R>* S, int M, uint64_t base,
+                                          const FusedGate& g, const Cx<R>* mp,
+                                          Cx<R>& tscale) {
+  using C = Cx<R>;
+  constexpr int PER = 16 / sizeof(C);
+  const int T = blockDim.x, tid = threadIdx.x;
+  if (g.kind == 0) {  // dense 2x2 on tile bit b0
+    const C m0 = mp[0], m1 = mp[1], m2 = mp[2], m3 = mp[3];
+    for (int j = tid; j < (M >> 1); j += T) {
+      const int i0 = (int)insert_zero((uint64_t)j, g.b0);
+      const int i1 = i0 | (1 << g.b0);
+      const int p0 = PER == 2 ? aswz(i0) : i0, p1 = PER == 2 ? aswz(i1) : i1;
+      const C x0 = S[p0], x1 = S[p1];
+      S[p0] = cmad(m1, x1, cmul(m0, x0));
+      S[p1] = cmad(m3, x1, cmul(m2, x0));
+    }
+  } else if (g.kind == 1) {  // dense 4x4 on tile bits b0 (MSB), b1
+    const int hi = g.b0 > g.b1 ? g.b0 : g.b1, lo = g.b0 > g.b1 ? g.b1 : g.b0;
+    const int M0 = 1 << g.b0, M1 = 1 << g.b1;
+    for (int j = tid; j < (M >> 2); j += T) {
+      const int i = (int)insert_zero(insert_zero((uint64_t)j, lo), hi);
+      int p[4] = {i, i | M1, i | M0, i | M0 | M1};
+      C v[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (PER == 2) p[k] = aswz(p[k]);
+        v[k] = S[p[k]];
+      }
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        C acc = cmul(mp[4 * r], v[0]);
+        acc = cmad(mp[4 * r + 1], v[1], acc);
+        acc = cmad(mp[4 * r + 2], v[2], acc);
+        acc = cmad(mp[4 * r + 3], v[3], acc);
+        S[p[r]] = acc;
+      }
+    }
+  } else {  // diagonal on nq qubits (tile bits or -1 - position)
+    int gidx = 0, lb0 = -1, lb1 = -1;
+    for (int q = 0; q < g.nq; ++q) {
+      const int b = q == 0 ? g.b0 : g.b1;
+      if (b < 0)
+        gidx |= (int)((base >> (-1 - b)) & 1) << (g.nq - 1 - q);
+      else if (q == 0)
+        lb0 = b;
+      else
+        lb1 = b;
+    }
+    if (lb0 < 0 && lb1 < 0) {
+      if (threadIdx.x == 0) tscale = cmul(tscale, mp[gidx]);
+      return;
+    }
+    for (int l = tid; l < M; l += T) {
+      int idx = gidx;
+      if (lb0 >= 0) idx |= ((l >> lb0) & 1) << (g.nq - 1);
+      if (lb1 >= 0) idx |= ((l >> lb1) & 1);
+      const int pl = PER == 2 ? aswz(l) : l;
+      S[pl] = cmul(mp[idx], S[pl]);
+    }
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(512, 1)
+    adjoint_stage_kernel(Cx<R>* psi, Cx<R>* lam, const Cx<R>* pool,
+                         AdjStageArgs a, double* partial) {
+  using C = Cx<R>;
+  constexpr int PER = 16 / sizeof(C);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int M = 1 << a.m;
+  C* SP = reinterpret_cast<C*>(smem_raw);
+  C* SL = SP + M;
+  __shared__ double red[16];
+  __shared__ C scale_sh;
+  const int T = blockDim.x, tid = threadIdx.x;
+  const uint64_t tiles_per_state = uint64_t(1) << (a.n - a.m);
+  const uint64_t s = blockIdx.x / tiles_per_state;
+  uint64_t base = blockIdx.x % tiles_per_state;
+  for (int j = 0; j < a.m; ++j) base = insert_zero(base, a.spos[j]);
+  C* gp = psi + (s << a.n) + base;
+  C* gl = lam + (s << a.n) + base;
+  const int run = 1 << a.c;
+  for (int l = tid * PER; l < M; l += T * PER) {
+    const int r = l >> a.c;
+    uint64_t off = (uint64_t)(l & (run - 1));
+    for (int j = 0; j < a.m - a.c; ++j)
+      if ((r >> j) & 1) off += uint64_t(1) << a.hpos[j];
+    const int pl = PER == 2 ? aswz(l) : l;
+    cp_async16<R>(&SP[pl], gp + off);
+    cp_async16<R>(&SL[pl], gl + off);
+  }
+  if (tid == 0) {
+    scale_sh.x = 1;
+    scale_sh.y = 0;
+  }
+  cp_async_wait_all();
+  __syncthreads();
+
+  for (int oi = 0; oi < a.num_ops; ++oi) {
+    const AdjOp& op = a.ops[oi];
+    if (op.kind == 1) {
+      if ((base & op.g.cmask) != op.g.cval) continue;
+      const C* mp = pool + op.g.mat + (int64_t)s * op.g.mat_bstride;
+      const bool all_global = op.g.kind == 2 && op.g.b0 < 0 &&
+                              (op.g.nq < 2 || op.g.b1 < 0);
+      if (all_global) {
+        // one factor per tile, applied once to both states at the store
+        if (tid == 0) {
+          int gidx = 0;
+          for (int q = 0; q < op.g.nq; ++q) {
+            const int b = q == 0 ? op.g.b0 : op.g.b1;
+            gidx |= (int)((base >> (-1 - b)) & 1) << (op.g.nq - 1 - q);
+          }
+          scale_sh = cmul(scale_sh, mp[gidx]);
+        }
+        continue;
+      }
+      adj_fixed<R>(SP, M, base, op.g, mp, scale_sh);
+      adj_fixed<R>(SL, M, base, op.g, mp, scale_sh);
+      __syncthreads();
+      continue;
+    }
+    const double th =
+        op.scale * (a.params_f64
+                        ? static_cast<const double*>(a.params)[s * a.num_params + op.pidx]
+                        : (double)static_cast<const float*>(a.params)[s * a.num_params + op.pidx]);
+    double sn, cs;
+    sincos(0.5 * th, &sn, &cs);
+    const R c = (R)cs, sr = (R)sn;
+    double gr = 0.0;
+    if (op.bit < 0) {
+      // Z on a bit outside the tile: the tile sits at z = +/-1
+      const int zb = (int)((base >> (-1 - op.bit)) & 1);
+      const double sgn = zb ? -1.0 : 1.0;
+      for (int l = tid; l < M; l += T) {
+        const int pl = PER == 2 ? aswz(l) : l;
+        const C p = SP[pl], q = SL[pl];
+        gr += sgn * ((double)q.x * p.y - (double)q.y * p.x);
+      }
+      if (tid == 0) {
+        // U^dag = diag(e^{+i th/2}, e^{-i th/2}) restricted to this tile
+        C f;
+        f.x = c;
+        f.y = zb ? -sr : sr;
+        scale_sh = cmul(scale_sh, f);
+        // a per-tile factor multiplies psi and lambda alike
+      }
+    } else {
+      const int b = op.bit;
+      for (int j = tid; j < (M >> 1); j += T) {
+        const int i0 = (int)insert_zero((uint64_t)j, b);
+        const int i1 = i0 | (1 << b);
+        const int p0 = PER == 2 ? aswz(i0) : i0, p1 = PER == 2 ? aswz(i1) : i1;
+        const C x0 = SP[p0], x1 = SP[p1], l0 = SL[p0], l1 = SL[p1];
+        C q0, q1, m0, m1;
+        if (op.gen == 0) {
+          gr += (double)l0.x * x1.y - (double)l0.y * x1.x +
+                (double)l1.x * x0.y - (double)l1.y * x0.x;
+          q0.x = c * x0.x - sr * x1.y; q0.y = c * x0.y + sr * x1.x;
+          q1.x = c * x1.x - sr * x0.y; q1.y = c * x1.y + sr * x0.x;
+          m0.x = c * l0.x - sr * l1.y; m0.y = c * l0.y + sr * l1.x;
+          m1.x = c * l1.x - sr * l0.y; m1.y = c * l1.y + sr * l0.x;
+        } else if (op.gen == 1) {
+          gr += -((double)l0.x * x1.x + (double)l0.y * x1.y) +
+                ((double)l1.x * x0.x + (double)l1.y * x0.y);
+          q0.x = c * x0.x + sr * x1.x; q0.y = c * x0.y + sr * x1.y;
+          q1.x = c * x1.x - sr * x0.x; q1.y = c * x1.y - sr * x0.y;
+          m0.x = c * l0.x + sr * l1.x; m0.y = c * l0.y + sr * l1.y;
+          m1.x = c * l1.x - sr * l0.x; m1.y = c * l1.y - sr * l0.y;
+        } else {
+          gr += (double)l0.x * x0.y - (double)l0.y * x0.x -
+                ((double)l1.x * x1.y - (double)l1.y * x1.x);
+          q0.x = c * x0.x - sr * x0.y; q0.y = c * x0.y + sr * x0.x;
+          q1.x = c * x1.x + sr * x1.y; q1.y = c * x1.y - sr * x1.x;
+          m0.x = c * l0.x - sr * l0.y; m0.y = c * l0.y + sr * l0.x;
+          m1.x = c * l1.x + sr * l1.y; m1.y = c * l1.y - sr * l1.x;
+        }
+        SP[p0] = q0;
+        SP[p1] = q1;
+        SL[p0] = m0;
+        SL[p1] = m1;
+      }
+    }
+    // block reduction of gr into partial[slot][tile]
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) gr += __shfl_xor_sync(0xffffffffu, gr, o);
+    if ((tid & 31) == 0) red[tid >> 5] = gr;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < (T >> 5); ++w) t += red[w];
+      partial[(uint64_t)op.slot * gridDim.x + blockIdx.x] = t;
+    }
+    __syncthreads();
+  }
+
+  __syncthreads();  // scale_sh may have been updated by thread 0 alone
+  const C sc = scale_sh;
+  const bool scaled = !(sc.x == 1 && sc.y == 0);
+  for (int l = tid * PER; l < M; l += T * PER) {
+    const int r = l >> a.c;
+    uint64_t off = (uint64_t)(l & (run - 1));
+    for (int j = 0; j < a.m - a.c; ++j)
+      if ((r >> j) & 1) off += uint64_t(1) << a.hpos[j];
+    const int pl = PER == 2 ? aswz(l) : l;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      C p = SP[pl + k], q = SL[pl + k];
+      if (scaled) {
+        p = cmul(sc, p);
+        q = cmul(sc, q);
+      }
+      gp[off + k] = p;
+      gl[off + k] = q;
+    }
+  }
+}
+
+// grad[s * P + pidx[slot]] += scale[slot] * sum over the state's tiles
+__global__ void adjoint_stage_finalize(const double* partial, int num_slots,
+                                       uint64_t tiles_per_state,
+                                       uint64_t num_tiles,
+                                       const int32_t* pidx,
+                                       const double* scale, double* grad,
+                                       int64_t num_params) {
+  const uint64_t item = blockIdx.x;  // slot * num_states + state
+  const uint64_t num_states = num_tiles / tiles_per_state;
+  const int slot = (int)(item / num_states);
+  const uint64_t s = item % num_states;
+  if (slot >= num_slots) return;
+  double acc = 0.0;
+  for (uint64_t t = threadIdx.x; t < tiles_per_state; t += blockDim.x)
+    acc += partial[(uint64_t)slot * num_tiles + s * tiles_per_state + t];
+  __shared__ double red[8];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    grad[s * num_params + pidx[slot]] += scale[slot] * t;
+  }
+}
+
+}  // namespace gbsv
+
+using namespace gbsv;
+
+extern "C" int gbsv_adjoint_stage(
+    void* psi, void* lam, int dtype, int num_qubits, int64_t num_states,
+    int tile_qubits, int contiguous_qubits, const int32_t* tile_positions,
+    const void* ops, int num_ops, const void* pool, const void* params,
+    int params_dtype, int64_t num_params, int num_slots,
+    const int32_t* slot_param, const double* slot_scale, double* grad,
+    void* scratch, size_t scratch_bytes, void* stream) {
+  if (dtype != GBSV_C64 && dtype != GBSV_C128)
+    return set_error(GBSV_ERR_INVALID_ARG, "state dtype must be complex");
+  if (params_dtype != GBSV_F32 && params_dtype != GBSV_F64)
+    return set_error(GBSV_ERR_INVALID_ARG, "params must be float32/float64");
+  const int n = num_qubits, m = tile_qubits, c = contiguous_qubits;
+  const int mmax = dtype == GBSV_C64 ? 13 : 12;
+  if (n < 1 || n > 62 || m < 1 || m > n || m > mmax ||
+      c < (dtype == GBSV_C64 ? 1 : 0) || c > m || num_states < 0 ||
+      num_ops < 0 || num_slots < 0 || num_params < 0)
+    return set_error(GBSV_ERR_INVALID_ARG,
+                     "bad adjoint stage n=%d m=%d c=%d", n, m, c);
+  if (num_states == 0) return GBSV_OK;
+  if (!psi || !lam || psi == lam || !tile_positions ||
+      (num_ops > 0 && (!ops || !pool)) ||
+      (num_slots > 0 && (!params || !slot_param || !slot_scale || !grad)))
+    return set_error(GBSV_ERR_INVALID_ARG, "null or aliased pointer");
+  AdjStageArgs a{};
+  a.n = n;
+  a.m = m;
+  a.c = c;
+  a.ops = static_cast<const AdjOp*>(ops);
+  a.num_ops = num_ops;
+  a.params = params;
+  a.params_f64 = params_dtype == GBSV_F64;
+  a.num_params = num_params;
+  uint64_t seen = 0;
+  for (int j = 0; j < m; ++j) {
+    const int p = tile_positions[j];
+    if (p < 0 || p >= n || ((seen >> p) & 1) || (j < c && p != j))
+      return set_error(GBSV_ERR_INVALID_ARG, "bad tile position %d", p);
+    seen |= uint64_t(1) << p;
+    if (j >= c) a.hpos[j - c] = p;
+    a.spos[j] = p;
+  }
+  for (int i = 1; i < m; ++i)
+    for (int j = i; j > 0 && a.spos[j - 1] > a.spos[j]; --j) {
+      const int t = a.spos[j];
+      a.spos[j] = a.spos[j - 1];
+      a.spos[j - 1] = t;
+    }
+  const uint64_t tiles_per_state = uint64_t(1) << (n - m);
+  const uint64_t tiles = (uint64_t)num_states * tiles_per_state;
+  if (tiles > 0x7fffffffull)
+    return set_error(GBSV_ERR_UNSUPPORTED, "too many tiles");
+  const size_t need = (size_t)num_slots * tiles * sizeof(double);
+  if (num_slots > 0 && (!scratch || scratch_bytes < need))
+    return set_error(GBSV_ERR_SCRATCH, "adjoint stage needs %zu scratch bytes",
+                     need);
+  const int amp = dtype_bytes(dtype);
+  const size_t smem = (size_t)2 * amp << m;
+  int threads = (1 << m) / 4;
+  if (threads > 512) threads = 512;
+  if (threads < 32) threads = 32;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  double* partial = static_cast<double*>(scratch);
+  if (dtype == GBSV_C64) {
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(adjoint_stage_kernel<float>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(2 * sizeof(float2) << mmax));
+      attr = true;
+    }
+    adjoint_stage_kernel<float><<<(unsigned)tiles, threads, smem, st>>>(
+        static_cast<float2*>(psi), static_cast<float2*>(lam),
+        static_cast<const float2*>(pool), a, partial);
+  } else {
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(adjoint_stage_kernel<double>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(2 * sizeof(double2) << mmax));
+      attr = true;
+    }
+    adjoint_stage_kernel<double><<<(unsigned)tiles, threads, smem, st>>>(
+        static_cast<double2*>(psi), static_cast<double2*>(lam),
+        static_cast<const double2*>(pool), a, partial);
+  }
+  int rc = after_launch("adjoint_stage_kernel");
+  if (rc || num_slots == 0) return rc;
+  const uint64_t items = (uint64_t)num_slots * num_states;
+  if (items > 0x7fffffffull)
+    return set_error(GBSV_ERR_UNSUPPORTED, "too many gradient slots");
+  adjoint_stage_finalize<<<(unsigned)items, 256, 0, st>>>(
+      partial, num_slots, tiles_per_state, tiles, slot_param, slot_scale,
+      grad, num_params);
+  return after_launch("adjoint_stage_finalize");
+}

@@ -91,6 +91,30 @@ __device__ __forceinline__ uint64_t insert_zero(uint64_t x, int pos) {
   return ((x >> pos) << (pos + 1)) | lo;
 }
 
+// Gate record of the fused stages (layout identical to gbsv_fused_gate_t).
+struct FusedGate {
+  int32_t kind;
+  int32_t nq;          // diagonal: number of qubits (1 or 2)
+  int32_t b0, b1;      // tile / register bit, or -1 - position outside
+  uint64_t cmask;      // apply only where (tile base & cmask) == cval
+  uint64_t cval;
+  int64_t mat;         // complex-element offset into the matrix pool
+  int64_t mat_bstride; // per-state stride in the pool (0 = shared)
+};
+
+// 16-byte asynchronous global -> shared copy (cp.async, L2 only).
+template <typename R>
+__device__ __forceinline__ void cp_async16(Cx<R>* smem, const Cx<R>* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s),
+               "l"(gmem)
+               : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 // --------------------------------------------------------------- host ----
 // Records a launch and converts a pending CUDA error into a status.
 int after_launch(const char* what);

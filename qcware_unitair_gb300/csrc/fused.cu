@@ -26,15 +26,6 @@ constexpr int FG_DENSE2 = 1;  // 4x4 on local bits b0 (matrix MSB), b1
 constexpr int FG_DIAG = 2;    // diagonal on 1-2 qubits, local or global
 constexpr int FG_MAX_TILE_BITS = 14;
 
-struct FusedGate {
-  int32_t kind;
-  int32_t nq;          // FG_DIAG: number of qubits (1 or 2)
-  int32_t b0, b1;      // local bit (>= 0) or, for FG_DIAG, -1 - global pos
-  uint64_t cmask;      // apply only where (tile base & cmask) == cval
-  uint64_t cval;
-  int64_t mat;         // complex-element offset into the matrix pool
-  int64_t mat_bstride; // per-state stride in the pool (0 = shared)
-};
 
 struct StageArgs {
   int n, m, c;
@@ -51,17 +42,6 @@ __device__ __forceinline__ int swz(int l) {
   return ((u ^ ((u >> 3) & 7)) << 1) | (l & 1);
 }
 
-template <typename R>
-__device__ __forceinline__ void cp_async16(Cx<R>* smem, const Cx<R>* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s),
-               "l"(gmem)
-               : "memory");
-}
-
-__device__ __forceinline__ void cp_async_wait_all() {
-  asm volatile("cp.async.wait_all;\n" ::: "memory");
-}
 
 // A stage's gates are copied into shared memory in chunks (records plus this
 // CTA's matrix values), so applying a gate never waits on global memory.

@@ -152,3 +152,24 @@ def test_c3_full_size_gradients_vs_finite_differences():
     a = np.array(errs)
     scale = np.abs(a[:, 1]).max()
     assert np.abs(a[:, 0] - a[:, 1]).max() / scale < 1e-4
+
+
+@pytest.mark.parametrize("n,layers,B,dtype", [(9, 3, 4, torch.complex128),
+                                              (14, 4, 3, torch.complex64),
+                                              (16, 2, 2, torch.complex64)])
+def test_fused_backward_matches_unfused(n, layers, B, dtype):
+    """Fused backward stages (tiles of psi and lambda, gradient partials per
+    tile) give the gradients of one-pass-per-gate adjoint steps."""
+    from qcware_unitair_gb300.adjoint import (_backward_fused,
+                                              _backward_sweep, _forward)
+    pc = hardware_efficient_ansatz(n, layers)
+    rng = np.random.default_rng(n)
+    params = torch.from_numpy(rng.normal(size=(B, pc.num_params))).to(DEV)
+    if dtype == torch.complex64:
+        params = params.float()
+    H = tfim(n)
+    psi_L, saved = _forward(pc, params, dtype, None, True)
+    g1 = _backward_fused(pc, params, H, psi_L, saved, dtype)
+    g2 = _backward_sweep(pc, params, H, psi_L, saved, dtype)
+    tol = 1e-10 if dtype == torch.complex128 else 2e-5
+    assert rel_err(g1.cpu(), g2.cpu()) < tol
