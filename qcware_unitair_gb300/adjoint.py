@@ -203,6 +203,85 @@ class ParamCircuit:
         return c
 
 
+# placeholder rotation matrices fix each rotation's record kind when a
+# forward program is planned once per circuit structure: a generic complex
+# 2x2 for X (dense), a real one for Y (real 2x2), a diagonal for Z
+_PLACEHOLDER = {
+    "X": torch.tensor([[0.6 + 0.2j, 0.1 - 0.3j], [0.4 + 0.1j, 0.7 - 0.2j]],
+                      dtype=torch.complex128),
+    "Y": torch.tensor([[0.8, -0.6], [0.6, 0.8]], dtype=torch.complex128),
+    "Z": torch.tensor([[0.6 - 0.8j, 0], [0, 0.6 + 0.8j]],
+                      dtype=torch.complex128),
+}
+
+
+def _forward_program(pc: ParamCircuit, a: int, b: int, B: int, dtype, dev,
+                     fuse: bool):
+    """(Program, scatter index, rotation index) for ops [a, b) with B
+    states, planned once per structure.  Each call only writes the rotation
+    values into the program's pool."""
+    key = (a, b, B, dtype, str(dev), fuse)
+    cache = pc.__dict__.setdefault("_fwd_cache", {})
+    if key in cache:
+        return cache[key]
+    c = Circuit(pc.num_qubits)
+    rots = []
+    for op in pc.ops[a:b]:
+        if op[0] == "fixed":
+            _, m, qs, kind = op
+            c.append(m, qs, kind)
+            continue
+        _, gen, q, p, scale = op
+        ph = _PLACEHOLDER[gen].expand(B, 2, 2).clone()
+        c.append(ph, [q], DIAG if gen == "Z" else DENSE)
+        rots.append((c.gates[-1], op))
+    prog = c.compile(dtype, dev, fuse=fuse, native=False)
+    idx, which = [], []
+    for g, op in rots:
+        if fuse:
+            off, nv = prog.gate_pool[id(g)]
+        else:
+            off, nv = None, 4
+        which.append((op[1], op[3], op[4], off, nv))
+    cache[key] = (prog, which, rots)
+    return cache[key]
+
+
+def _rotation_values(which, params, B, dtype):
+    """All rotations' pool entries, flattened in ``which`` order (rotation,
+    state, entry), from a handful of vectorised tensor ops."""
+    dev = params.device
+    cached = _rotation_values._meta.get(id(which))
+    if cached is None or cached[0] is not which:
+        gen = torch.tensor(["XYZ".index(w[0]) for w in which], device=dev)
+        pidx = torch.tensor([w[1] for w in which], device=dev)
+        half = torch.tensor([0.5 * w[2] for w in which], dtype=torch.float64,
+                            device=dev)
+        nv = torch.tensor([w[4] for w in which], device=dev)
+        keep = (torch.arange(4, device=dev)[None, None, :] <
+                nv[:, None, None]).expand(len(which), B, 4)
+        cached = (which, gen, pidx, half, nv, keep)
+        _rotation_values._meta[id(which)] = cached
+    _, gen, pidx, half, nv, keep = cached
+    th = params[:, pidx].to(torch.float64) * half          # (B, R)
+    c, s = torch.cos(th).T, torch.sin(th).T                 # (R, B)
+    z = torch.zeros_like(c)
+    isx, isy = (gen == 0)[:, None], (gen == 1)[:, None]
+    isz4 = ((gen == 2) & (nv == 4))[:, None]
+    # entry k of each rotation, real and imaginary parts (R, B)
+    re0, im0 = c, torch.where(isx | isy, z, -s)
+    re1 = torch.where(isy, -s, torch.where(isx | isz4, z, c))
+    im1 = torch.where(isx, -s, torch.where(isy | isz4, z, s))
+    re2, im2 = torch.where(isy, s, z), torch.where(isx, -s, z)
+    re3, im3 = c, torch.where(isz4, s, z)
+    re = torch.stack([re0, re1, re2, re3], -1)
+    im = torch.stack([im0, im1, im2, im3], -1)
+    return torch.complex(re, im).to(dtype)[keep]
+
+
+_rotation_values._meta = {}
+
+
 def _initial_state(n, B, dtype, device, psi0):
     if psi0 is None:
         s = torch.zeros(B, 2 ** n, dtype=dtype, device=device)
@@ -221,13 +300,28 @@ def _forward(pc: ParamCircuit, params, dtype, psi0, checkpoints: bool,
     dev = params.device
     psi = _initial_state(n, B, dtype, dev, psi0)
     saved = []
+    p = params.detach()
     for a, b in pc.segments():
         if checkpoints:
             saved.append(psi.clone())
-        if b > a:
+        if b <= a:
+            continue
+        if not fuse:
             prog = pc._segment_circuit(a, b, params, dtype).compile(
-                dtype, dev, fuse=fuse)
+                dtype, dev, fuse=False)
             prog.run(psi, inplace=True)
+            continue
+        prog, which, _ = _forward_program(pc, a, b, B, dtype, dev, fuse)
+        if which:
+            # one scatter of every rotation's values into the cached pool
+            idx = prog.__dict__.get("_rot_index")
+            if idx is None:
+                parts = [torch.arange(off, off + B * nv, device=dev)
+                         for _, _, _, off, nv in which]
+                idx = prog._rot_index = torch.cat(parts)
+            prog.pool.index_copy_(0, idx, _rotation_values(which, p, B,
+                                                           dtype))
+        prog.run(psi, inplace=True)
     return psi, saved
 
 

@@ -42,20 +42,21 @@ __global__ void __launch_bounds__(256)
        i < total; i += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t x = i & nmask;
     const Cx<R>* p = psi + (i - x);
-    double ar = 0.0, ai = 0.0;
+    // computed in the state's precision: the result is stored there
+    R ar = 0, ai = 0;
     for (int k = 0; k < num_terms; ++k) {
       const uint64_t y = x ^ st[k].xmask;
       // (X^xm Z^zm)|y> = (-1)^popc(y & zm) |y ^ xm>, so
       // (P psi)[x] = c * (-1)^popc(y & zm) * psi[y] with y = x ^ xm
       const Cx<R> v = p[y];
-      const double sgn = (__popcll(y & st[k].zmask) & 1) ? -1.0 : 1.0;
-      const double cr = sgn * st[k].re, ci = sgn * st[k].im;
-      ar += cr * (double)v.x - ci * (double)v.y;
-      ai += cr * (double)v.y + ci * (double)v.x;
+      const R sgn = (__popcll(y & st[k].zmask) & 1) ? R(-1) : R(1);
+      const R cr = sgn * (R)st[k].re, ci = sgn * (R)st[k].im;
+      ar = fma(cr, v.x, fma(-ci, v.y, ar));
+      ai = fma(cr, v.y, fma(ci, v.x, ai));
     }
     Cx<R> o;
-    o.x = (R)ar;
-    o.y = (R)ai;
+    o.x = ar;
+    o.y = ai;
     out[i] = o;
   }
 }
@@ -97,24 +98,28 @@ __global__ void __launch_bounds__(ADJ_THREADS)
   const int64_t lo = (int64_t)part * a.part_len;
   int64_t hi = lo + a.part_len;
   if (hi > a.pairs) hi = a.pairs;
-  double gr = 0.0;  // accumulates Im <lambda|P|psi>
+  Acc<R> gacc;  // accumulates Im <lambda|P|psi>
   for (int64_t j = lo + threadIdx.x; j < hi; j += ADJ_THREADS) {
     const uint64_t i0 = insert_zero((uint64_t)j, a.pos);
     const uint64_t i1 = i0 | (uint64_t(1) << a.pos);
     const C p0 = ps[i0], p1 = ps[i1], l0 = ls[i0], l1 = ls[i1];
     // <lambda|P|psi> restricted to the pair, imaginary part only
-    double im;
     if (a.gen == 0) {  // conj(l0) p1 + conj(l1) p0
-      im = (double)l0.x * p1.y - (double)l0.y * p1.x + (double)l1.x * p0.y -
-           (double)l1.y * p0.x;
+      gacc.add_prod(l0.x, p1.y);
+      gacc.add_prod(-l0.y, p1.x);
+      gacc.add_prod(l1.x, p0.y);
+      gacc.add_prod(-l1.y, p0.x);
     } else if (a.gen == 1) {  // conj(l0)(-i p1) + conj(l1)(i p0)
-      im = -((double)l0.x * p1.x + (double)l0.y * p1.y) +
-           ((double)l1.x * p0.x + (double)l1.y * p0.y);
+      gacc.add_prod(l1.x, p0.x);
+      gacc.add_prod(l1.y, p0.y);
+      gacc.add_prod(-l0.x, p1.x);
+      gacc.add_prod(-l0.y, p1.y);
     } else {  // conj(l0) p0 - conj(l1) p1
-      im = (double)l0.x * p0.y - (double)l0.y * p0.x -
-           ((double)l1.x * p1.y - (double)l1.y * p1.x);
+      gacc.add_prod(l0.x, p0.y);
+      gacc.add_prod(-l0.y, p0.x);
+      gacc.add_prod(-l1.x, p1.y);
+      gacc.add_prod(l1.y, p1.x);
     }
-    gr += im;
     C q0, q1, m0, m1;
     if (a.gen == 0) {  // [[c, i s], [i s, c]]
       q0.x = c * p0.x - sr * p1.y; q0.y = c * p0.y + sr * p1.x;
@@ -138,7 +143,7 @@ __global__ void __launch_bounds__(ADJ_THREADS)
     ls[i1] = m1;
   }
   __shared__ double sh[ADJ_THREADS / 32];
-  gr = warp_sum_adj(gr);
+  double gr = warp_sum_adj(gacc.value());
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = gr;
   __syncthreads();
   if (threadIdx.x < 32) {
@@ -303,6 +308,7 @@ struct AdjStageArgs {
   const void* params;
   int params_f64;
   int64_t num_params;
+  int num_slots;
 };
 
 __device__ __forceinline__ int aswz(int l) {
@@ -374,7 +380,7 @@ __device__ __forceinline__ void adj_fixed(Cx<R>* S, int M, uint64_t base,
 }
 
 template <typename R>
-__global__ void __launch_bounds__(512, 1)
+__global__ void __launch_bounds__(512, sizeof(R) == 4 ? 2 : 1)
     adjoint_stage_kernel(Cx<R>* psi, Cx<R>* lam, const Cx<R>* pool,
                          AdjStageArgs a, double* partial) {
   using C = Cx<R>;
@@ -383,7 +389,8 @@ __global__ void __launch_bounds__(512, 1)
   const int M = 1 << a.m;
   C* SP = reinterpret_cast<C*>(smem_raw);
   C* SL = SP + M;
-  __shared__ double red[16];
+  // per-warp gradient partials of every rotation: wred[slot * warps + w]
+  double* wred = reinterpret_cast<double*>(SL + M);
   __shared__ C scale_sh;
   const int T = blockDim.x, tid = threadIdx.x;
   const uint64_t tiles_per_state = uint64_t(1) << (a.n - a.m);
@@ -440,15 +447,16 @@ __global__ void __launch_bounds__(512, 1)
     double sn, cs;
     sincos(0.5 * th, &sn, &cs);
     const R c = (R)cs, sr = (R)sn;
-    double gr = 0.0;
+    Acc<R> gacc;
     if (op.bit < 0) {
       // Z on a bit outside the tile: the tile sits at z = +/-1
       const int zb = (int)((base >> (-1 - op.bit)) & 1);
-      const double sgn = zb ? -1.0 : 1.0;
+      const R sgn = zb ? R(-1) : R(1);
       for (int l = tid; l < M; l += T) {
         const int pl = PER == 2 ? aswz(l) : l;
         const C p = SP[pl], q = SL[pl];
-        gr += sgn * ((double)q.x * p.y - (double)q.y * p.x);
+        gacc.add_prod(sgn * q.x, p.y);
+        gacc.add_prod(-sgn * q.y, p.x);
       }
       if (tid == 0) {
         // U^dag = diag(e^{+i th/2}, e^{-i th/2}) restricted to this tile
@@ -467,22 +475,28 @@ __global__ void __launch_bounds__(512, 1)
         const C x0 = SP[p0], x1 = SP[p1], l0 = SL[p0], l1 = SL[p1];
         C q0, q1, m0, m1;
         if (op.gen == 0) {
-          gr += (double)l0.x * x1.y - (double)l0.y * x1.x +
-                (double)l1.x * x0.y - (double)l1.y * x0.x;
+          gacc.add_prod(l0.x, x1.y);
+          gacc.add_prod(-l0.y, x1.x);
+          gacc.add_prod(l1.x, x0.y);
+          gacc.add_prod(-l1.y, x0.x);
           q0.x = c * x0.x - sr * x1.y; q0.y = c * x0.y + sr * x1.x;
           q1.x = c * x1.x - sr * x0.y; q1.y = c * x1.y + sr * x0.x;
           m0.x = c * l0.x - sr * l1.y; m0.y = c * l0.y + sr * l1.x;
           m1.x = c * l1.x - sr * l0.y; m1.y = c * l1.y + sr * l0.x;
         } else if (op.gen == 1) {
-          gr += -((double)l0.x * x1.x + (double)l0.y * x1.y) +
-                ((double)l1.x * x0.x + (double)l1.y * x0.y);
+          gacc.add_prod(l1.x, x0.x);
+          gacc.add_prod(l1.y, x0.y);
+          gacc.add_prod(-l0.x, x1.x);
+          gacc.add_prod(-l0.y, x1.y);
           q0.x = c * x0.x + sr * x1.x; q0.y = c * x0.y + sr * x1.y;
           q1.x = c * x1.x - sr * x0.x; q1.y = c * x1.y - sr * x0.y;
           m0.x = c * l0.x + sr * l1.x; m0.y = c * l0.y + sr * l1.y;
           m1.x = c * l1.x - sr * l0.x; m1.y = c * l1.y - sr * l0.y;
         } else {
-          gr += (double)l0.x * x0.y - (double)l0.y * x0.x -
-                ((double)l1.x * x1.y - (double)l1.y * x1.x);
+          gacc.add_prod(l0.x, x0.y);
+          gacc.add_prod(-l0.y, x0.x);
+          gacc.add_prod(-l1.x, x1.y);
+          gacc.add_prod(l1.y, x1.x);
           q0.x = c * x0.x - sr * x0.y; q0.y = c * x0.y + sr * x0.x;
           q1.x = c * x1.x + sr * x1.y; q1.y = c * x1.y - sr * x1.x;
           m0.x = c * l0.x - sr * l0.y; m0.y = c * l0.y + sr * l0.x;
@@ -494,17 +508,21 @@ __global__ void __launch_bounds__(512, 1)
         SL[p1] = m1;
       }
     }
-    // block reduction of gr into partial[slot][tile]
+    // warp partial now; the block reduction waits for the end of the stage
+    double gr = gacc.value();
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) gr += __shfl_xor_sync(0xffffffffu, gr, o);
-    if ((tid & 31) == 0) red[tid >> 5] = gr;
-    __syncthreads();
-    if (tid == 0) {
+    if ((tid & 31) == 0) wred[op.slot * (T >> 5) + (tid >> 5)] = gr;
+    __syncthreads();  // the next op reads amplitudes this one wrote
+  }
+  // one block reduction for all rotations of the stage
+  {
+    const int warps = T >> 5;
+    for (int k = tid; k < a.num_slots; k += T) {
       double t = 0.0;
-      for (int w = 0; w < (T >> 5); ++w) t += red[w];
-      partial[(uint64_t)op.slot * gridDim.x + blockIdx.x] = t;
+      for (int w = 0; w < warps; ++w) t += wred[k * warps + w];
+      partial[(uint64_t)k * gridDim.x + blockIdx.x] = t;
     }
-    __syncthreads();
   }
 
   __syncthreads();  // scale_sh may have been updated by thread 0 alone
@@ -592,6 +610,7 @@ extern "C" int gbsv_adjoint_stage(
   a.params = params;
   a.params_f64 = params_dtype == GBSV_F64;
   a.num_params = num_params;
+  a.num_slots = num_slots;
   uint64_t seen = 0;
   for (int j = 0; j < m; ++j) {
     const int p = tile_positions[j];
@@ -616,10 +635,15 @@ extern "C" int gbsv_adjoint_stage(
     return set_error(GBSV_ERR_SCRATCH, "adjoint stage needs %zu scratch bytes",
                      need);
   const int amp = dtype_bytes(dtype);
-  const size_t smem = (size_t)2 * amp << m;
   int threads = (1 << m) / 4;
   if (threads > 512) threads = 512;
   if (threads < 32) threads = 32;
+  const size_t smem =
+      ((size_t)2 * amp << m) + (size_t)num_slots * (threads / 32) * 8;
+  if (smem > 200 * 1024)
+    return set_error(GBSV_ERR_UNSUPPORTED,
+                     "adjoint stage with %d rotations needs %zu bytes of "
+                     "shared memory", num_slots, smem);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   double* partial = static_cast<double*>(scratch);
   if (dtype == GBSV_C64) {
@@ -627,7 +651,7 @@ extern "C" int gbsv_adjoint_stage(
     if (!attr) {
       cudaFuncSetAttribute(adjoint_stage_kernel<float>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(2 * sizeof(float2) << mmax));
+                           200 * 1024);
       attr = true;
     }
     adjoint_stage_kernel<float><<<(unsigned)tiles, threads, smem, st>>>(
@@ -638,7 +662,7 @@ extern "C" int gbsv_adjoint_stage(
     if (!attr) {
       cudaFuncSetAttribute(adjoint_stage_kernel<double>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(2 * sizeof(double2) << mmax));
+                           200 * 1024);
       attr = true;
     }
     adjoint_stage_kernel<double><<<(unsigned)tiles, threads, smem, st>>>(

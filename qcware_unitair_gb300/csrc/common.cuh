@@ -85,6 +85,41 @@ __device__ __forceinline__ void store_chunk(double2* p, const double2* r) {
   for (int j = 0; j < V; ++j) __stcs(p + j, r[j]);
 }
 
+// Per-thread accumulator for reductions.  GB300 issues FP64 at a small
+// fraction of its FP32 rate, so complex64 data is accumulated per thread as
+// an unevaluated float pair (hi, lo): each product a*b enters exactly
+// (p = a*b, its rounding error e = fma(a, b, -p)) and each addition keeps
+// its rounding error (TwoSum, Knuth), so the per-thread result carries
+// about twice float precision (near FP64) using only FP32 operations.  Only
+// the per-thread results meet in FP64.  complex128 data uses FP64.
+template <typename R> struct Acc;
+template <> struct Acc<float> {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float s = hi + x;
+    const float bp = s - hi;
+    lo += (hi - (s - bp)) + (x - bp);
+    hi = s;
+  }
+  // += a * b exactly
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    const float p = a * b;
+    lo += fmaf(a, b, -p);
+    add(p);
+  }
+  __device__ __forceinline__ double value() const {
+    return (double)hi + (double)lo;
+  }
+};
+template <> struct Acc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double x) { s += x; }
+  __device__ __forceinline__ void add_prod(double a, double b) {
+    s = fma(a, b, s);
+  }
+  __device__ __forceinline__ double value() const { return s; }
+};
+
 // Insert a zero bit at position pos of x (bits >= pos move up by one).
 __device__ __forceinline__ uint64_t insert_zero(uint64_t x, int pos) {
   uint64_t lo = x & ((uint64_t(1) << pos) - 1);

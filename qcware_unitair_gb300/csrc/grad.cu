@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(OG_THREADS)
   const int64_t lo = (int64_t)p * a.part_len;
   int64_t hi = lo + a.part_len;
   if (hi > a.groups) hi = a.groups;
-  double x = 0.0, y = 0.0;
+  Acc<R> ax, ay;
   for (int64_t t = lo + threadIdx.x; t < hi; t += OG_THREADS) {
     uint64_t base = (uint64_t)t;
     for (int j = 0; j < a.k; ++j) {
@@ -65,11 +65,12 @@ __global__ void __launch_bounds__(OG_THREADS)
     const Cx<R> u = gs[base + oa];
     const Cx<R> v = ps[base + oc];
     // u * conj(v)
-    x = fma((double)u.x, (double)v.x, x);
-    x = fma((double)u.y, (double)v.y, x);
-    y = fma((double)u.y, (double)v.x, y);
-    y = fma(-(double)u.x, (double)v.y, y);
+    ax.add_prod(u.x, v.x);
+    ax.add_prod(u.y, v.y);
+    ay.add_prod(u.y, v.x);
+    ay.add_prod(-u.x, v.y);
   }
+  double x = ax.value(), y = ay.value();
   __shared__ double sx[OG_THREADS / 32], sy[OG_THREADS / 32];
   x = warp_sum_og(x);
   y = warp_sum_og(y);

@@ -90,12 +90,13 @@ __global__ void __launch_bounds__(256)
   const Cx<R>* p = psi + c * CHUNK;
   const uint64_t len = dim - c * CHUNK < (uint64_t)CHUNK ? dim - c * CHUNK
                                                          : (uint64_t)CHUNK;
-  double acc = 0.0;
+  Acc<R> a;
   for (int i = threadIdx.x; i < (int)len; i += blockDim.x) {
     const Cx<R> v = p[i];
-    acc = fma((double)v.x, (double)v.x, acc);
-    acc = fma((double)v.y, (double)v.y, acc);
+    a.add_prod(v.x, v.x);
+    a.add_prod(v.y, v.y);
   }
+  double acc = a.value();
   __shared__ double sh[8];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);

@@ -12,6 +12,7 @@
 // and a second kernel sums the partials of each row in a fixed order, so the
 // result is deterministic (no atomics).
 #include <mutex>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -114,13 +115,13 @@ __global__ void __launch_bounds__(RED_THREADS)
   int64_t hi = lo + part_len;
   if (hi > dim) hi = dim;
   const Cx<R>* p = psi + row * dim;
-  double acc = 0.0;
+  Acc<R> acc;
   for (int64_t i = lo + threadIdx.x; i < hi; i += RED_THREADS) {
     const Cx<R> v = __ldcs(p + i);
-    acc = fma((double)v.x, (double)v.x, acc);
-    acc = fma((double)v.y, (double)v.y, acc);
+    acc.add_prod(v.x, v.x);
+    acc.add_prod(v.y, v.y);
   }
-  const double2 s = block_sum2(acc, 0.0);
+  const double2 s = block_sum2(acc.value(), 0.0);
   if (threadIdx.x == 0) {
     if (parts == 1) {
       if (out_f64)
@@ -172,17 +173,17 @@ __global__ void __launch_bounds__(RED_THREADS)
   const int64_t lo = (int64_t)part * ra.part_len;
   int64_t hi = lo + ra.part_len;
   if (hi > ra.dim) hi = ra.dim;
-  double x = 0.0, y = 0.0;
+  Acc<R> x, y;
   for (int64_t i = lo + threadIdx.x; i < hi; i += RED_THREADS) {
     const Cx<R> u = a[oa + i * ra.ia];
     const Cx<R> v = b[ob + i * ra.ib];
     // conj(u) * v
-    x = fma((double)u.x, (double)v.x, x);
-    x = fma((double)u.y, (double)v.y, x);
-    y = fma((double)u.x, (double)v.y, y);
-    y = fma(-(double)u.y, (double)v.x, y);
+    x.add_prod(u.x, v.x);
+    x.add_prod(u.y, v.y);
+    y.add_prod(u.x, v.y);
+    y.add_prod(-u.y, v.x);
   }
-  const double2 s = block_sum2(x, y);
+  const double2 s = block_sum2(x.value(), y.value());
   if (threadIdx.x == 0) {
     if (ra.parts == 1) {
       if (out_dtype == GBSV_C64)
@@ -208,14 +209,17 @@ __global__ void __launch_bounds__(RED_THREADS)
   const int64_t lo = (int64_t)part * ra.part_len;
   int64_t hi = lo + ra.part_len;
   if (hi > ra.dim) hi = ra.dim;
-  double acc = 0.0;
+  // diag * |psi|^2 in the state's precision (FP64 when either input is)
+  using W = typename std::conditional<(sizeof(RD) > sizeof(R)), RD, R>::type;
+  Acc<W> acc;
   for (int64_t i = lo + threadIdx.x; i < hi; i += RED_THREADS) {
-    const double w = (double)d[oa + i * ra.ia];
+    const W w = (W)d[oa + i * ra.ia];
     const Cx<R> v = psi[ob + i * ra.ib];
-    const double p = fma((double)v.x, (double)v.x, (double)v.y * (double)v.y);
-    acc = fma(w, p, acc);
+    const W x = (W)v.x, y = (W)v.y;
+    acc.add_prod(w * x, x);
+    acc.add_prod(w * y, y);
   }
-  const double2 s = block_sum2(acc, 0.0);
+  const double2 s = block_sum2(acc.value(), 0.0);
   if (threadIdx.x == 0) {
     if (ra.parts == 1) {
       if (out_dtype == GBSV_F32)

@@ -599,7 +599,9 @@ class Program:
         pool_parts = []
         pool_len = 0
 
-        def add_pool(values: torch.Tensor):
+        self.gate_pool = {}  # id(gate) -> (pool offset, values per state)
+
+        def add_pool(values: torch.Tensor, gate=None):
             """values (nv,) or (B, nv) -> (offset, bstride).  Host values
             stay on the host until one transfer at the end."""
             nonlocal pool_len
@@ -607,6 +609,8 @@ class Program:
             off = pool_len
             pool_parts.append(v.reshape(-1))
             pool_len += v.numel()
+            if gate is not None:
+                self.gate_pool[id(gate)] = (off, v.shape[-1])
             return off, (v.shape[1] if v.dim() == 2 else 0)
 
         self.ops = []
@@ -635,7 +639,7 @@ class Program:
                     kreg = {b: k for k, b in enumerate(rbits)}
                     for g in lgates:
                         rec, vals = _record(g, n, local, kreg, self.rb)
-                        off, bstride = add_pool(vals)
+                        off, bstride = add_pool(vals, g)
                         rec["mat"], rec["mat_bstride"] = off, bstride
                         records.append(rec)
                     lay = np.zeros((), dtype=LAYOUT_DTYPE)
@@ -648,7 +652,7 @@ class Program:
             first = len(records)
             for g in st.gates:
                 rec, vals = _record(g, n, local, None)
-                off, bstride = add_pool(vals)
+                off, bstride = add_pool(vals, g)
                 rec["mat"], rec["mat_bstride"] = off, bstride
                 records.append(rec)
             self.ops.append(("stage", c, positions, first, len(st.gates)))
