@@ -85,14 +85,21 @@ __global__ void __launch_bounds__(ADJ_THREADS)
   using C = Cx<R>;
   const int64_t s = blockIdx.x / a.parts;
   const int part = blockIdx.x % a.parts;
-  const double theta =
-      a.angle_scale * (a.angle_f64
-                           ? static_cast<const double*>(a.angles)[s * a.angle_stride]
-                           : (double)static_cast<const float*>(a.angles)[s * a.angle_stride]);
-  double sn, cs;
-  sincos(0.5 * theta, &sn, &cs);
-  // U^dag = exp(+i theta/2 P) = cos I + i sin P
-  const R c = (R)cs, sr = (R)sn;
+  // U^dag = exp(+i theta/2 P) = cos I + i sin P; one FP64 sincos per block
+  __shared__ R cs_sh[2];
+  if (threadIdx.x == 0) {
+    const double theta =
+        a.angle_scale *
+        (a.angle_f64
+             ? static_cast<const double*>(a.angles)[s * a.angle_stride]
+             : (double)static_cast<const float*>(a.angles)[s * a.angle_stride]);
+    double sn, cs;
+    sincos(0.5 * theta, &sn, &cs);
+    cs_sh[0] = (R)cs;
+    cs_sh[1] = (R)sn;
+  }
+  __syncthreads();
+  const R c = cs_sh[0], sr = cs_sh[1];
   C* ps = psi + (s << a.n);
   C* ls = lam + (s << a.n);
   const int64_t lo = (int64_t)part * a.part_len;
@@ -413,6 +420,21 @@ __global__ void __launch_bounds__(512, sizeof(R) == 4 ? 2 : 1)
     scale_sh.x = 1;
     scale_sh.y = 0;
   }
+  // cos and sin of every rotation of the stage, once per CTA: FP64 sincos
+  // on one thread per rotation instead of on every thread
+  R* csn = reinterpret_cast<R*>(wred + a.num_slots * (T >> 5));
+  for (int oi = tid; oi < a.num_ops; oi += T) {
+    const AdjOp& op = a.ops[oi];
+    if (op.kind != 0) continue;
+    const double th =
+        op.scale * (a.params_f64
+                        ? static_cast<const double*>(a.params)[s * a.num_params + op.pidx]
+                        : (double)static_cast<const float*>(a.params)[s * a.num_params + op.pidx]);
+    double sn, cs;
+    sincos(0.5 * th, &sn, &cs);
+    csn[2 * op.slot] = (R)cs;
+    csn[2 * op.slot + 1] = (R)sn;
+  }
   cp_async_wait_all();
   __syncthreads();
 
@@ -440,13 +462,7 @@ __global__ void __launch_bounds__(512, sizeof(R) == 4 ? 2 : 1)
       __syncthreads();
       continue;
     }
-    const double th =
-        op.scale * (a.params_f64
-                        ? static_cast<const double*>(a.params)[s * a.num_params + op.pidx]
-                        : (double)static_cast<const float*>(a.params)[s * a.num_params + op.pidx]);
-    double sn, cs;
-    sincos(0.5 * th, &sn, &cs);
-    const R c = (R)cs, sr = (R)sn;
+    const R c = csn[2 * op.slot], sr = csn[2 * op.slot + 1];
     Acc<R> gacc;
     if (op.bit < 0) {
       // Z on a bit outside the tile: the tile sits at z = +/-1
@@ -638,8 +654,9 @@ extern "C" int gbsv_adjoint_stage(
   int threads = (1 << m) / 4;
   if (threads > 512) threads = 512;
   if (threads < 32) threads = 32;
-  const size_t smem =
-      ((size_t)2 * amp << m) + (size_t)num_slots * (threads / 32) * 8;
+  const size_t smem = ((size_t)2 * amp << m) +
+                      (size_t)num_slots * (threads / 32) * 8 +
+                      (size_t)num_slots * amp;
   if (smem > 200 * 1024)
     return set_error(GBSV_ERR_UNSUPPORTED,
                      "adjoint stage with %d rotations needs %zu bytes of "
