@@ -294,6 +294,148 @@ def bench_adjoint(dev, n=20, layers=12, batch=256, small_batch=8):
             "grad_rel_diff_vs_autograd": agree}
 
 
+# ------------------------------------------------------- small-state configs
+def _cuda_time(fn, reps):
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def bench_c0(dev):
+    """12 qubits x 64 random states, complex64, 200 canonical gates: the
+    plain per-gate path (apply_operator per gate) against the whole circuit
+    as one fused launch (each state is one 4096-amplitude tile)."""
+    import torch
+    import qcware_unitair_gb300 as ug
+    from qcware_unitair_gb300.circuits import random_circuit, random_states
+    from qcware_unitair_gb300.fusion import Circuit
+    n, B, G = 12, 64, 200
+    gates = random_circuit(n, G, seed=0)
+    psi0 = random_states(n, (B,), torch.complex64, seed=0).to(dev)
+    mats = [torch.from_numpy(g.matrix()).to(dev, torch.complex64)
+            for g in gates]
+
+    def plain():
+        st = psi0
+        for g, m in zip(gates, mats):
+            st = ug.apply_operator(m, g.qubits, st)
+        return ug.norm_squared(st)
+
+    prog = Circuit.from_gates(n, gates).compile(torch.complex64, dev)
+
+    def fused():
+        return ug.norm_squared(prog.run(psi0))
+
+    a = plain()
+    b = fused()
+    return {"workload": "12 qubits x 64 states, complex64, 200 random gates, "
+                        "final states and norms",
+            "plain_ms": round(_cuda_time(plain, 5), 3),
+            "fused_ms": round(_cuda_time(fused, 20), 4),
+            "fused_launches": prog.num_passes + 1,
+            "max_norm_diff": float((a - b).abs().max())}
+
+
+def bench_c2(dev, layers=100):
+    """4096 states x 16 qubits (batch (64, 64)), complex64: 100 layers of
+    per-state RX, RY, RZ on every qubit (angles (64, 64, 16) ~ U[0, 2pi))
+    and a CNOT ladder i -> i+1.  The fused layer program is captured once
+    as a CUDA graph of all layers and replayed; the plain path launches one
+    kernel per gate.  Plus the broadcast case: one 16-qubit state under
+    4096 gate batches."""
+    import math
+    import torch
+    import qcware_unitair_gb300 as ug
+    from qcware_unitair_gb300.adjoint import (ParamCircuit, _forward_program,
+                                              _rotation_values)
+    from qcware_unitair_gb300.circuits import random_states
+    n, B = 16, 4096
+    pc = ParamCircuit(n, 3 * n)
+    for q in range(n):
+        pc.rx(q, 3 * q)
+        pc.ry(q, 3 * q + 1)
+        pc.rz(q, 3 * q + 2)
+    for q in range(n - 1):
+        pc.cnot(q, q + 1)
+    g = torch.Generator(device=dev)
+    g.manual_seed(0)
+    angles = torch.rand(layers, B, 3 * n, generator=g, device=dev,
+                        dtype=torch.float32) * (2 * math.pi)
+    psi0 = random_states(n, (B,), torch.complex64, seed=2).to(dev)
+    prog, which, _ = _forward_program(pc, 0, len(pc.ops), B,
+                                      torch.complex64, dev, True)
+    idx = torch.cat([torch.arange(off, off + B * nv, device=dev)
+                     for _, _, _, off, nv in which])
+    vals = torch.stack([_rotation_values(which, angles[l], B,
+                                         torch.complex64)
+                        for l in range(layers)])
+    psi = psi0.clone()
+
+    def circuit():
+        for l in range(layers):
+            prog.pool.index_copy_(0, idx, vals[l])
+            prog.run(psi, inplace=True)
+
+    circuit()  # warm-up outside capture
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    stream = torch.cuda.Stream(dev)
+    stream.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(stream):
+        with torch.cuda.graph(graph, stream=stream):
+            circuit()
+    torch.cuda.current_stream(dev).wait_stream(stream)
+
+    def replay():
+        psi.copy_(psi0)
+        graph.replay()
+
+    graph_ms = _cuda_time(replay, 3)
+    fused_out = psi.clone()
+    # plain path: one kernel per gate, per-state 2x2 matrices
+    rx = ug.gates.rx
+    ry = ug.gates.ry
+    rz = ug.gates.rz
+    cnot = ug.gates.cnot(device=dev)
+
+    def plain():
+        st = psi0
+        for l in range(layers):
+            a = angles[l].view(B, n, 3)
+            for q in range(n):
+                st = ug.apply_operator(rx(a[:, q, 0]), [q], st)
+                st = ug.apply_operator(ry(a[:, q, 1]), [q], st)
+                st = ug.apply_operator(rz(a[:, q, 2]), [q], st)
+            for q in range(n - 1):
+                st = ug.apply_operator(cnot, [q, q + 1], st)
+        return st
+
+    plain_out = plain()
+    diff = float((plain_out - fused_out).abs().max())
+    plain_ms = _cuda_time(plain, 1)
+    # broadcast: one state, 4096 operator batches
+    one = psi0[0].contiguous()
+    ops = rx(angles[0].view(B, n, 3)[:, 0, 0])
+    bc_ms = _cuda_time(lambda: ug.apply_operator(ops, [0], one), 10)
+    bc_bytes = 2 ** n * 8 * (1 + B)
+    return {"workload": f"4096 x 16 qubits complex64, {layers} layers of "
+                        "per-state RX, RY, RZ on every qubit + CNOT ladder",
+            "graph_ms": round(graph_ms, 2), "plain_ms": round(plain_ms, 1),
+            "speedup": round(plain_ms / graph_ms, 2),
+            "passes_per_layer": prog.num_passes,
+            "max_abs_diff_fused_vs_plain": diff,
+            "broadcast_1x4096_ms": round(bc_ms, 4),
+            "broadcast_GBs": round(bc_bytes / (bc_ms / 1e3) / 1e9, 1)}
+
+
 # ---------------------------------------------------------------- serving --
 def bench_serving(dev, num=300, rate=150.0, qubits=(10, 22)):
     """The serving trace (Poisson arrivals; qubits, depth 20-500 and 1-64
@@ -500,6 +642,8 @@ def run_gpu(args, ws, rank, local):
         "clocks": clocks.summary(),
     }
     if not args.no_extras:
+        result["c0_12q_x64"] = bench_c0(dev)
+        result["c2_16q_x4096"] = bench_c2(dev)
         result["adjoint"] = bench_adjoint(dev)
         result["serving"] = bench_serving(dev)
     if rank == 0 and not args.no_cpu_baseline:
