@@ -22,21 +22,35 @@ import importlib
 
 import torch
 
-from . import simulation, states
+from . import measurement, simulation, states
+
+# unitair.simulation.operations functions replaced by the engine (same
+# signatures, operations.py:15-805).
+_OPERATIONS = {
+    "apply_operator": simulation.apply_operator,
+    "apply_all_qubits": simulation.apply_all_qubits,
+    "apply_phase": simulation.apply_phase,
+    "act_first_qubits": simulation.act_first_qubits,
+    "act_last_qubit": simulation.act_last_qubit,
+    "apply_to_qubits": simulation.apply_to_qubits,
+    "swap": simulation.swap,
+    "permute_qubits": simulation.permute_qubits,
+    "roll_qubits": simulation.roll_qubits,
+    "multi_cz": simulation.multi_cz,
+    "multi_controlled_z": simulation.multi_controlled_z,
+    "multi_controlled_x": simulation.multi_controlled_x,
+}
+_SIM_EXPORTS = ("apply_operator", "apply_all_qubits", "apply_phase",
+                "act_first_qubits", "act_last_qubit", "apply_to_qubits",
+                "swap", "multi_cz", "multi_controlled_z",
+                "multi_controlled_x")
 
 _TARGETS = {
-    "unitair.simulation.operations": {
-        "apply_operator": simulation.apply_operator,
-        "apply_all_qubits": simulation.apply_all_qubits,
-        "apply_phase": simulation.apply_phase,
-        "act_first_qubits": simulation.act_first_qubits,
-    },
-    "unitair.simulation": {
-        "apply_operator": simulation.apply_operator,
-        "apply_all_qubits": simulation.apply_all_qubits,
-        "apply_phase": simulation.apply_phase,
-        "act_first_qubits": simulation.act_first_qubits,
-    },
+    "unitair.simulation.operations": dict(_OPERATIONS),
+    "unitair.simulation": dict(
+        {k: _OPERATIONS[k] for k in _SIM_EXPORTS},
+        measure=measurement.measure),
+    "unitair.simulation.measurement": {"measure": measurement.measure},
     "unitair.states.innerprod": {
         "inner_product": states.inner_product,
         "norm_squared": states.norm_squared,
@@ -60,16 +74,31 @@ _TARGETS = {
 _saved: dict = {}
 
 
+def _has_cpu_tensor(x) -> bool:
+    if isinstance(x, torch.Tensor):
+        return not x.is_cuda
+    if isinstance(x, (list, tuple)):
+        return any(_has_cpu_tensor(v) for v in x)
+    return False
+
+
+def _to(x, device):
+    if isinstance(x, torch.Tensor):
+        return x.to(device)
+    if isinstance(x, (list, tuple)):
+        return type(x)(_to(v, device) for v in x)
+    return x
+
+
 def _mover(fn, device):
     @functools.wraps(fn)
-    def wrapper(*args):
-        cpu = any(isinstance(a, torch.Tensor) and not a.is_cuda for a in args)
-        if not cpu:
-            return fn(*args)
-        moved = [a.to(device) if isinstance(a, torch.Tensor) else a
-                 for a in args]
-        out = fn(*moved)
-        return out.to("cpu") if isinstance(out, torch.Tensor) else out
+    def wrapper(*args, **kwargs):
+        if not (_has_cpu_tensor(args) or _has_cpu_tensor(list(
+                kwargs.values()))):
+            return fn(*args, **kwargs)
+        out = fn(*_to(args, device),
+                 **{k: _to(v, device) for k, v in kwargs.items()})
+        return _to(out, "cpu")
     return wrapper
 
 
