@@ -592,54 +592,6 @@ __device__ __forceinline__ void ts_anti1(C* v, const C* mm) {
   }
 }
 
-// 4x4 on register bits K0 (matrix MSB) and K1; entries are read at each use
-// (volatile) so the 16 values never occupy registers.
-template <typename C, int NR, int K0, int K1>
-__device__ __forceinline__ void ts_dense2(C* v, const C* mm_) {
-  const volatile C* mm = mm_;
-#pragma unroll
-  for (int i = 0; i < NR; ++i) {
-    if ((i >> K0) & 1 || (i >> K1) & 1) continue;
-    const int idx[4] = {i, i | (1 << K1), i | (1 << K0),
-                        i | (1 << K0) | (1 << K1)};
-    C x[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) x[k] = v[idx[k]];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      C acc = czero<C>();
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        C e;
-        e.x = mm[4 * r + k].x;
-        e.y = mm[4 * r + k].y;
-        acc = cmad(e, x[k], acc);
-      }
-      v[idx[r]] = acc;
-    }
-  }
-}
-
-template <typename C, int NR, int K0, int K1>
-__device__ __forceinline__ void ts_perm2(C* v, int code) {
-  const int s0 = code & 3, s1 = (code >> 2) & 3, s2 = (code >> 4) & 3,
-            s3 = (code >> 6) & 3;
-#pragma unroll
-  for (int i = 0; i < NR; ++i) {
-    if ((i >> K0) & 1 || (i >> K1) & 1) continue;
-    const int idx[4] = {i, i | (1 << K1), i | (1 << K0),
-                        i | (1 << K0) | (1 << K1)};
-    const C x0 = v[idx[0]], x1 = v[idx[1]], x2 = v[idx[2]], x3 = v[idx[3]];
-    auto pick = [&](int q) {
-      return q == 0 ? x0 : q == 1 ? x1 : q == 2 ? x2 : x3;
-    };
-    v[idx[0]] = pick(s0);
-    v[idx[1]] = pick(s1);
-    v[idx[2]] = pick(s2);
-    v[idx[3]] = pick(s3);
-  }
-}
-
 template <typename C, int NR, int K0, int K1>
 __device__ __forceinline__ void ts_swap2(C* v) {
 #pragma unroll
@@ -664,8 +616,63 @@ __device__ __forceinline__ void ts_cx2(C* v) {
 }
 
 template <typename C>
+__device__ __forceinline__ C sel4(const C* pm, int i) {
+  const C lo = (i & 1) ? pm[1] : pm[0];
+  const C hi = (i & 1) ? pm[3] : pm[2];
+  return (i & 2) ? hi : lo;
+}
+
+template <typename C>
 __device__ __forceinline__ bool is_one(const C& f) {
   return f.x == 1 && f.y == 0;
+}
+
+// 4x4 (dense, or a permutation given by code) on register bits k0 (matrix
+// MSB) and k1 known only at run time: the registers go through a local
+// copy that is indexed at run time, so the register array itself is only
+// ever indexed by constants.
+template <typename C, int NR>
+__device__ __noinline__ void ts_generic2_mem(C* t, int k0, int k1, bool dense,
+                                             int code, const C* mm) {
+  const int b0 = 1 << k0, b1 = 1 << k1;
+  for (int i = 0; i < NR; ++i) {
+    if (i & (b0 | b1)) continue;
+    const int idx[4] = {i, i | b1, i | b0, i | b0 | b1};
+    C x[4];
+    for (int k = 0; k < 4; ++k) x[k] = t[idx[k]];
+    for (int r = 0; r < 4; ++r) {
+      if (dense) {
+        C acc = czero<C>();
+        for (int k = 0; k < 4; ++k) acc = cmad(mm[4 * r + k], x[k], acc);
+        t[idx[r]] = acc;
+      } else {
+        t[idx[r]] = x[(code >> (2 * r)) & 3];
+      }
+    }
+  }
+}
+
+template <typename C, int NR>
+__device__ __forceinline__ void ts_generic2(C* v, int k0, int k1, bool dense,
+                                            int code, const C* mm) {
+  C t[NR];
+#pragma unroll
+  for (int i = 0; i < NR; ++i) t[i] = v[i];
+  ts_generic2_mem<C, NR>(t, k0, k1, dense, code, mm);
+#pragma unroll
+  for (int i = 0; i < NR; ++i) v[i] = t[i];
+}
+
+// diagonal on register bits k0 (index MSB), k1 known at run time
+template <typename C, int NR>
+__device__ __forceinline__ void ts_diag2_any(C* v, int k0, int k1,
+                                             const C* d) {
+#pragma unroll
+  for (int i = 0; i < NR; ++i) {
+    const int idx = (((i >> k0) & 1) << 1) | ((i >> k1) & 1);
+    const C f = sel4(d, idx);
+    if (!is_one(f)) v[i] = cmul(f, v[i]);
+  }
 }
 
 // diag(f0, f1) on register bit K
@@ -679,22 +686,6 @@ __device__ __forceinline__ void ts_diag1(C* v, const C& f0, const C& f1) {
     } else if (!one0) {
       v[i] = cmul(f0, v[i]);
     }
-  }
-}
-
-template <typename C, int NR, int K0, int K1>
-__device__ __forceinline__ void ts_diag2(C* v, const C* d) {
-  bool one[4];
-  C f[4];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    f[j] = d[j];
-    one[j] = is_one(f[j]);
-  }
-#pragma unroll
-  for (int i = 0; i < NR; ++i) {
-    const int idx = (((i >> K0) & 1) << 1) | ((i >> K1) & 1);
-    if (!one[idx]) v[i] = cmul(f[idx], v[i]);
   }
 }
 
@@ -751,13 +742,6 @@ __device__ __forceinline__ void ts_load_vals(C* pm, const C* src) {
   }
 }
 
-template <typename C>
-__device__ __forceinline__ C sel4(const C* pm, int i) {
-  const C lo = (i & 1) ? pm[1] : pm[0];
-  const C hi = (i & 1) ? pm[3] : pm[2];
-  return (i & 2) ? hi : lo;
-}
-
 // Apply one decoded operation to a thread's registers.
 template <typename R, int RB>
 __device__ __forceinline__ void ts_apply(Cx<R>* v, const TOp& o,
@@ -795,11 +779,10 @@ __device__ __forceinline__ void ts_apply(Cx<R>* v, const TOp& o,
         break;
     }
   } else if (op < TOP_DIAG1) {
-    if (op < TOP_PERM2) {
-      const C* m16 = mats + o.moff;
-      switch (op - TOP_DENSE2) { TS_PS(0, (ts_dense2<C, NR, K0, K1>(v, m16))) }
-    } else if (op < TOP_SWAP2) {
-      switch (op - TOP_PERM2) { TS_PS(0, (ts_perm2<C, NR, K0, K1>(v, o.code))) }
+    if (op < TOP_SWAP2) {  // general 4x4 or permutation: rare, not unrolled
+      const int p = op < TOP_PERM2 ? op - TOP_DENSE2 : op - TOP_PERM2;
+      const int k0 = p >> 2, j = p & 3, k1 = j < k0 ? j : j + 1;
+      ts_generic2<C, NR>(v, k0, k1, op < TOP_PERM2, o.code, mats + o.moff);
     } else if (op < TOP_CX2) {
       switch (op - TOP_SWAP2) { TS_PS(0, (ts_swap2<C, NR, K0, K1>(v))) }
     } else {
@@ -809,7 +792,9 @@ __device__ __forceinline__ void ts_apply(Cx<R>* v, const TOp& o,
     const C f0 = sel4(pm, fixed), f1 = sel4(pm, fixed | o.code);
     switch (op - TOP_DIAG1) { TS_KS(0, (ts_diag1<C, NR, K>(v, f0, f1))) }
   } else if (op < TOP_SCALAR) {
-    switch (op - TOP_DIAG2) { TS_PS(0, (ts_diag2<C, NR, K0, K1>(v, mm))) }
+    const int p = op - TOP_DIAG2;
+    const int k0 = p >> 2, j = p & 3, k1 = j < k0 ? j : j + 1;
+    ts_diag2_any<C, NR>(v, k0, k1, pm);
   } else if (op == TOP_SCALAR) {
     ts = cmul(ts, sel4(pm, fixed));
   }

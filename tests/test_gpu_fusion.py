@@ -146,3 +146,41 @@ def test_30q_fused_matches_plain():
     torch.cuda.empty_cache()
     assert diff < 1e-5
     assert abs(norm - 1) < 1e-5
+
+
+def _haar(rng, d):
+    z = rng.standard_normal((d, d)) + 1j * rng.standard_normal((d, d))
+    q, r = np.linalg.qr(z)
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.complex64, 1e-5),
+                                       (torch.complex128, 1e-12)])
+@pytest.mark.parametrize("n", [9, 12, 14])
+def test_general_two_qubit_ops_in_stages(oracle, dtype, tol, n):
+    """Dense 4x4 unitaries, non-SWAP/CNOT permutations and two-qubit
+    diagonals inside register layouts (the run-time-indexed paths)."""
+    rng = np.random.default_rng(100 + n)
+    circ = Circuit(n)
+    perms = [[0, 3, 1, 2], [1, 0, 3, 2], [3, 2, 1, 0], [2, 0, 3, 1]]
+    for i in range(150):
+        a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+        kind = i % 5
+        if kind == 0:
+            circ.append(_haar(rng, 4), [a, b], "dense")
+        elif kind == 1:
+            p = perms[int(rng.integers(len(perms)))]
+            circ.append(np.eye(4)[p].astype(complex), [a, b], "dense")
+        elif kind == 2:
+            ph = np.exp(1j * rng.uniform(0, 2 * np.pi, 4))
+            circ.append(np.diag(ph), [a, b], "diag")
+        elif kind == 3:
+            circ.h(a)
+        else:
+            circ.append(_haar(rng, 2), [a], "dense")
+    psi0 = random_states(n, (2,), dtype, seed=n)
+    prog = circ.compile(dtype, DEV, tile_qubits=min(n, 12))
+    assert prog.num_passes < len(circ)
+    out = prog.run(psi0.to(DEV))
+    ref = oracle_run(oracle, circ, psi0.numpy())
+    assert max_err(out.cpu().numpy(), ref) <= tol
