@@ -438,6 +438,8 @@ struct TLayout {
   int32_t first, count;
   int32_t nscal;               // leading operations that are thread scalars
   int32_t spo[LAYOUT_MAX_RB];  // swizzled tile offsets of the register bits
+  int32_t spw[LAYOUT_MAX_RB];  // the same for the write-back (relabelled)
+  int32_t cw;                  // write-back offset of flipped register bits
   uint16_t lo_s[32], hi_s[16]; // swizzled offsets of thread bits 0-4 / 5-8
   uint16_t lo_r[32], hi_r[16]; // the same, plain
 };
@@ -537,6 +539,82 @@ __device__ TOp ts_decode(const FusedGate& g, int moff, const int32_t* rb) {
     default: break;
   }
   return o;
+}
+
+// Value permutations applied when a gate's matrix values are copied in.
+constexpr int VP_REV4 = 4;      // 2x2 conjugated by X: entries reversed
+constexpr int VP_XOR4X4 = 8;    // 4x4 conjugated by X on bits F (low 2)
+constexpr int VP_XORDIAG = 16;  // diagonal values indexed by i ^ F
+
+// Rewrite a decoded operation on logical register bits onto physical bits
+// of the relabelling (perm, flip); X and SWAP only update the relabelling.
+// Returns whether an operation remains to run; vm receives the value
+// permutation its matrix needs.
+template <int RB>
+__device__ bool ts_relabel(TOp& o, int* perm, int& flip, int8_t& vm) {
+  const int op = o.op;
+  const bool cond = o.x != 0 || o.a != 0;
+  auto pair_of = [](int p, int& k0, int& k1) {
+    k0 = p >> 2;
+    const int j = p & 3;
+    k1 = j < k0 ? j : j + 1;
+  };
+  if (op < TOP_DENSE2) {  // one register bit
+    const int fam = op / 5, k = op - 5 * fam;
+    const int pk = perm[k];
+    const bool fl = (flip >> pk) & 1;
+    if (fam == TOP_SWAP1 / 5 && !cond) {  // X: complement the bit
+      flip ^= 1 << pk;
+      return false;
+    }
+    o.op = (int16_t)(5 * fam + pk);
+    if (fl && fam != TOP_SWAP1 / 5) vm = VP_REV4;
+    return true;
+  }
+  if (op < TOP_DIAG1) {  // two register bits
+    const int base = op < TOP_PERM2 ? TOP_DENSE2
+                     : op < TOP_SWAP2 ? TOP_PERM2
+                     : op < TOP_CX2 ? TOP_SWAP2
+                                    : TOP_CX2;
+    int k0, k1;
+    pair_of(op - base, k0, k1);
+    const int p0 = perm[k0], p1 = perm[k1];
+    const int F = (((flip >> p0) & 1) << 1) | ((flip >> p1) & 1);
+    if (base == TOP_SWAP2 && !cond) {
+      perm[k0] = p1;
+      perm[k1] = p0;
+      return false;
+    }
+    o.op = (int16_t)(base + pair_index(p0, p1));
+    if (base == TOP_CX2) {
+      // control complemented: flip the target everywhere as well
+      if (F & 2) flip ^= 1 << p1;
+    } else if (base == TOP_DENSE2 && F) {
+      vm = (int8_t)(VP_XOR4X4 | F);
+    } else if (base == TOP_PERM2 && F) {
+      int code = 0;
+      for (int r = 0; r < 4; ++r)
+        code |= (((o.code >> (2 * (r ^ F))) & 3) ^ F) << (2 * r);
+      o.code = (int16_t)code;
+    }
+    return true;
+  }
+  if (op < TOP_DIAG2) {  // diagonal with one register bit
+    const int pk = perm[op - TOP_DIAG1];
+    o.op = (int16_t)(TOP_DIAG1 + pk);
+    if ((flip >> pk) & 1) vm = (int8_t)(VP_XORDIAG | o.code);
+    return true;
+  }
+  if (op < TOP_SCALAR) {  // diagonal on two register bits
+    int k0, k1;
+    pair_of(op - TOP_DIAG2, k0, k1);
+    const int p0 = perm[k0], p1 = perm[k1];
+    const int F = (((flip >> p0) & 1) << 1) | ((flip >> p1) & 1);
+    o.op = (int16_t)(TOP_DIAG2 + pair_index(p0, p1));
+    if (F) vm = (int8_t)(VP_XORDIAG | F);
+    return true;
+  }
+  return op != TOP_NOP;
 }
 
 // ----------------------------------------------------- register kernels --
@@ -846,8 +924,7 @@ __global__ void __launch_bounds__(RB >= 5 ? 256 : 512, 1)
   __shared__ TLayout lay[TS_MAXL];
   __shared__ uint64_t offh[NIT];
   __shared__ int16_t nv[TS_MAXG];   // values per gate, then their offsets
-  __shared__ int16_t dst[TS_MAXG];  // slot of each gate's operation
-  __shared__ int8_t scal[TS_MAXG];
+  __shared__ int8_t vp[TS_MAXG];    // value permutation of each gate
   __shared__ int sh_total;
 
   const int T = blockDim.x;
@@ -918,10 +995,12 @@ __global__ void __launch_bounds__(RB >= 5 ? 256 : 512, 1)
       }
     } else if (e < 48 + RB) {
       dst.spo[e - 48] = swz_amp<R>(1 << ly.rb[e - 48]);
+      dst.spw[e - 48] = dst.spo[e - 48];
     } else if (e == 48 + RB) {
       dst.first = ly.first_gate - g0;
       dst.count = ly.num_gates;
       dst.nscal = 0;
+      dst.cw = 0;
     }
   };
   constexpr int LE = 48 + RB + 1;  // table entries per layout
@@ -939,35 +1018,61 @@ __global__ void __launch_bounds__(RB >= 5 ? 256 : 512, 1)
       const int k = fg_nvals(g.kind, g.nq);
       const C* src = pool + g.mat + (int64_t)s * g.mat_bstride;
       const int mo = nv[gi];
-      for (int j = 0; j < k; ++j) mats[mo + j] = src[j];
+      const int vm = vp[gi];  // value permutation from relabelling
+      if (vm == 0) {
+        for (int j = 0; j < k; ++j) mats[mo + j] = src[j];
+      } else if (vm == VP_REV4) {
+        for (int j = 0; j < 4; ++j) mats[mo + j] = src[3 - j];
+      } else if (vm & VP_XOR4X4) {
+        const int F = vm & 3;
+        for (int j = 0; j < 16; ++j)
+          mats[mo + j] = src[4 * ((j >> 2) ^ F) + ((j & 3) ^ F)];
+      } else {  // VP_XORDIAG
+        const int F = vm & 3;
+        for (int j = 0; j < k; ++j) mats[mo + j] = src[j ^ F];
+      }
     }
   };
   uint64_t loaded_s = t0 / tps;
   if (resident) {
-    // Thread scalars commute with everything a layout does, so each
-    // layout's scalars move to its front and run in a short loop of their
-    // own: decode, then place (scalars first, order kept), then store.
-    auto decode = [&](int gi) {
-      int li = 0;
-      while (li + 1 < L && a.layouts[li + 1].first_gate <= g0 + gi) ++li;
-      return ts_decode<RB>(gates[gi], nv[gi], a.layouts[li].rb);
-    };
-    for (int gi = tid; gi < G; gi += T) {
-      scal[gi] = decode(gi).op == TOP_SCALAR;
-      dst[gi] = -1;
-    }
-    __syncthreads();
+    // One thread per layout walks its gates in order.
+    //  * Thread scalars commute with everything a layout does: they move to
+    //    the layout's front and run in a short loop of their own.
+    //  * X and SWAP on register bits move no data: the layout keeps a
+    //    relabelling (logical register bit k lives in physical bit perm[k],
+    //    physical bits in `flip` hold complemented values); later
+    //    operations are rewritten onto physical bits (matrix values
+    //    permuted to match, vp) and the write-back uses the final map.
+    __syncthreads();  // layout tables
     for (int li = tid; li < L; li += T) {
       const int f = lay[li].first, cnt = lay[li].count;
+      const int32_t* rb = a.layouts[li].rb;
       int ns = 0;
-      for (int j = f; j < f + cnt; ++j) ns += scal[j];
+      for (int j = f; j < f + cnt; ++j)
+        ns += ts_decode<RB>(gates[j], nv[j], rb).op == TOP_SCALAR;
       int ps = f, po = f + ns;
-      for (int j = f; j < f + cnt; ++j) dst[j] = (int16_t)(scal[j] ? ps++ : po++);
+      int perm[RB];
+      for (int k = 0; k < RB; ++k) perm[k] = k;
+      int flip = 0;
+      for (int j = f; j < f + cnt; ++j) {
+        TOp o = ts_decode<RB>(gates[j], nv[j], rb);
+        vp[j] = 0;
+        if (o.op == TOP_SCALAR) {
+          ops[ps++] = o;
+          continue;
+        }
+        if (ts_relabel<RB>(o, perm, flip, vp[j])) ops[po++] = o;
+      }
+      lay[li].count = po - f;
       lay[li].nscal = ns;
+      // physical bit b holds logical bit k with perm[k] == b
+      int cw = 0;
+      for (int k = 0; k < RB; ++k) {
+        lay[li].spw[perm[k]] = lay[li].spo[k];
+        if ((flip >> perm[k]) & 1) cw ^= lay[li].spo[k];
+      }
+      lay[li].cw = cw;
     }
-    __syncthreads();
-    for (int gi = tid; gi < G; gi += T)
-      if (dst[gi] >= 0) ops[dst[gi]] = decode(gi);
     __syncthreads();
     load_values(loaded_s);
   }
@@ -1057,8 +1162,18 @@ __global__ void __launch_bounds__(RB >= 5 ? 256 : 512, 1)
 #pragma unroll
         for (int i = 0; i < NR; ++i) v[i] = cmul(ts, v[i]);
       }
+      // write-back through the final relabelling of register bits
 #pragma unroll
-      for (int i = 0; i < NR; ++i) S[addr(i)] = v[i];
+      for (int k = 0; k < RB; ++k) sp[k] = ly.spw[k];
+      const int sbw = sb ^ ly.cw;
+#pragma unroll
+      for (int i = 0; i < NR; ++i) {
+        int x = sbw;
+#pragma unroll
+        for (int k = 0; k < RB; ++k)
+          if ((i >> k) & 1) x ^= sp[k];
+        S[x] = v[i];
+      }
       __syncthreads();
     }
 

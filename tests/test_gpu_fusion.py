@@ -184,3 +184,46 @@ def test_general_two_qubit_ops_in_stages(oracle, dtype, tol, n):
     out = prog.run(psi0.to(DEV))
     ref = oracle_run(oracle, circ, psi0.numpy())
     assert max_err(out.cpu().numpy(), ref) <= tol
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.complex64, 1e-5),
+                                       (torch.complex128, 1e-12)])
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_x_and_swap_heavy_stages(oracle, dtype, tol, seed):
+    """X and SWAP on register bits only relabel registers; every other
+    operation after them (dense, controlled, permutation, diagonal) must
+    see the relabelled bits."""
+    rng = np.random.default_rng(seed)
+    n = 10
+    circ = Circuit(n)
+    for _ in range(150):
+        a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+        k = int(rng.integers(10))
+        if k == 0:
+            circ.x(a)
+        elif k == 1:
+            circ.swap(a, b)
+        elif k == 2:
+            circ.cnot(a, b)
+        elif k == 3:
+            circ.append(_haar(rng, 2), [a], "dense")
+        elif k == 4:
+            circ.append(_haar(rng, 4), [a, b], "dense")
+        elif k == 5:
+            circ.append(np.diag(np.exp(1j * rng.uniform(0, 6, 4))), [a, b],
+                        "diag")
+        elif k == 6:
+            circ.append(gate_matrix("RZ", float(rng.uniform(0, 6))), [a],
+                        "diag")
+        elif k == 7:
+            circ.h(a)
+        elif k == 8:
+            circ.y(a)
+        else:
+            circ.append(np.eye(4)[[1, 3, 0, 2]].astype(complex), [a, b],
+                        "dense")
+    psi0 = random_states(n, (2,), dtype, seed=seed)
+    prog = circ.compile(dtype, DEV, tile_qubits=10)
+    out = prog.run(psi0.to(DEV))
+    ref = oracle_run(oracle, circ, psi0.numpy())
+    assert max_err(out.cpu().numpy(), ref) <= tol
