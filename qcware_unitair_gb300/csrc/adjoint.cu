@@ -79,6 +79,24 @@ __device__ __forceinline__ double warp_sum_adj(double v) {
   return v;
 }
 
+// Warp sum of float values carried as an unevaluated pair (hi, lo): each
+// butterfly step adds the partner's pair with TwoSum, so the result keeps
+// about twice float precision with FP32 operations only (GB300 issues FP64
+// at a small fraction of its FP32 rate).  Every lane ends with the same
+// pair; the caller converts one lane's pair to double.
+__device__ __forceinline__ void warp_sum_pair(float& hi, float& lo) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+    const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+    const float s = hi + oh;
+    const float bp = s - hi;
+    const float e = (hi - (s - bp)) + (oh - bp);
+    lo = lo + ol + e;
+    hi = s;
+  }
+}
+
 template <typename R>
 __global__ void __launch_bounds__(ADJ_THREADS)
     adjoint_rot_kernel(Cx<R>* psi, Cx<R>* lam, AdjArgs a, double* partial) {
@@ -463,7 +481,9 @@ __global__ void __launch_bounds__(512, sizeof(R) == 4 ? 2 : 1)
       continue;
     }
     const R c = csn[2 * op.slot], sr = csn[2 * op.slot + 1];
-    Acc<R> gacc;
+    // a thread sums only its few pairs of the tile (plain FMA); precision
+    // is kept where the sums grow: across lanes, warps and tiles
+    R gsum = 0;
     if (op.bit < 0) {
       // Z on a bit outside the tile: the tile sits at z = +/-1
       const int zb = (int)((base >> (-1 - op.bit)) & 1);
@@ -471,8 +491,8 @@ __global__ void __launch_bounds__(512, sizeof(R) == 4 ? 2 : 1)
       for (int l = tid; l < M; l += T) {
         const int pl = PER == 2 ? aswz(l) : l;
         const C p = SP[pl], q = SL[pl];
-        gacc.add_prod(sgn * q.x, p.y);
-        gacc.add_prod(-sgn * q.y, p.x);
+        gsum = fma(sgn * q.x, p.y, gsum);
+        gsum = fma(-sgn * q.y, p.x, gsum);
       }
       if (tid == 0) {
         // U^dag = diag(e^{+i th/2}, e^{-i th/2}) restricted to this tile
@@ -491,28 +511,28 @@ __global__ void __launch_bounds__(512, sizeof(R) == 4 ? 2 : 1)
         const C x0 = SP[p0], x1 = SP[p1], l0 = SL[p0], l1 = SL[p1];
         C q0, q1, m0, m1;
         if (op.gen == 0) {
-          gacc.add_prod(l0.x, x1.y);
-          gacc.add_prod(-l0.y, x1.x);
-          gacc.add_prod(l1.x, x0.y);
-          gacc.add_prod(-l1.y, x0.x);
+          gsum = fma(l0.x, x1.y, gsum);
+          gsum = fma(-l0.y, x1.x, gsum);
+          gsum = fma(l1.x, x0.y, gsum);
+          gsum = fma(-l1.y, x0.x, gsum);
           q0.x = c * x0.x - sr * x1.y; q0.y = c * x0.y + sr * x1.x;
           q1.x = c * x1.x - sr * x0.y; q1.y = c * x1.y + sr * x0.x;
           m0.x = c * l0.x - sr * l1.y; m0.y = c * l0.y + sr * l1.x;
           m1.x = c * l1.x - sr * l0.y; m1.y = c * l1.y + sr * l0.x;
         } else if (op.gen == 1) {
-          gacc.add_prod(l1.x, x0.x);
-          gacc.add_prod(l1.y, x0.y);
-          gacc.add_prod(-l0.x, x1.x);
-          gacc.add_prod(-l0.y, x1.y);
+          gsum = fma(l1.x, x0.x, gsum);
+          gsum = fma(l1.y, x0.y, gsum);
+          gsum = fma(-l0.x, x1.x, gsum);
+          gsum = fma(-l0.y, x1.y, gsum);
           q0.x = c * x0.x + sr * x1.x; q0.y = c * x0.y + sr * x1.y;
           q1.x = c * x1.x - sr * x0.x; q1.y = c * x1.y - sr * x0.y;
           m0.x = c * l0.x + sr * l1.x; m0.y = c * l0.y + sr * l1.y;
           m1.x = c * l1.x - sr * l0.x; m1.y = c * l1.y - sr * l0.y;
         } else {
-          gacc.add_prod(l0.x, x0.y);
-          gacc.add_prod(-l0.y, x0.x);
-          gacc.add_prod(-l1.x, x1.y);
-          gacc.add_prod(l1.y, x1.x);
+          gsum = fma(l0.x, x0.y, gsum);
+          gsum = fma(-l0.y, x0.x, gsum);
+          gsum = fma(-l1.x, x1.y, gsum);
+          gsum = fma(l1.y, x1.x, gsum);
           q0.x = c * x0.x - sr * x0.y; q0.y = c * x0.y + sr * x0.x;
           q1.x = c * x1.x + sr * x1.y; q1.y = c * x1.y - sr * x1.x;
           m0.x = c * l0.x - sr * l0.y; m0.y = c * l0.y + sr * l0.x;
@@ -525,10 +545,15 @@ __global__ void __launch_bounds__(512, sizeof(R) == 4 ? 2 : 1)
       }
     }
     // warp partial now; the block reduction waits for the end of the stage
-    double gr = gacc.value();
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) gr += __shfl_xor_sync(0xffffffffu, gr, o);
-    if ((tid & 31) == 0) wred[op.slot * (T >> 5) + (tid >> 5)] = gr;
+    if constexpr (sizeof(R) == 4) {
+      float hi = gsum, lo = 0.f;
+      warp_sum_pair(hi, lo);
+      if ((tid & 31) == 0)
+        wred[op.slot * (T >> 5) + (tid >> 5)] = (double)hi + (double)lo;
+    } else {
+      const double gr = warp_sum_adj(gsum);
+      if ((tid & 31) == 0) wred[op.slot * (T >> 5) + (tid >> 5)] = gr;
+    }
     __syncthreads();  // the next op reads amplitudes this one wrote
   }
   // one block reduction for all rotations of the stage
