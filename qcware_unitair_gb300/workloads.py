@@ -1,0 +1,116 @@
+"""Small, fixed workloads for timing and profiling the kernels one at a time.
+
+    python -m qcware_unitair_gb300.workloads stage 26          # random circuit
+    python -m qcware_unitair_gb300.workloads gates 24 H 64     # one stage, 64 H
+    python -m qcware_unitair_gb300.workloads adjoint 16        # 20q ansatz grad
+
+Each runs its workload twice (a warm-up, then a CUDA-event-timed run) and
+prints one line; under a profiler, skip the first run's launches.
+
+``stage``: the canonical random circuit (``circuits.random_circuit``, numpy
+seed 0) on n qubits, 200 gates, complex64, compiled into fused stages and run
+in place from |0...0>.
+
+``gates``: one fused stage on n qubits holding 8 Hadamards on spread tile
+bits plus k copies of one gate kind (H, X, RX, or RZout = RZ on a bit that is
+never a register bit), for the per-gate cost of the stage kernel.
+
+``adjoint``: forward + adjoint backward of the 20-qubit, 12-layer
+hardware-efficient ansatz (RY, RZ per qubit, CZ ring) at the given batch,
+loss mean(<sum Z> + 0.5 <sum XX>).
+"""
+from __future__ import annotations
+
+import sys
+
+import torch
+
+
+def _timed(fn):
+    fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def stage(n: int = 26, gates: int = 200) -> float:
+    from .circuits import random_circuit, zero_state
+    from .fusion import Circuit
+    dev = torch.device("cuda")
+    prog = Circuit.from_gates(n, random_circuit(n, gates, seed=0)).compile(
+        torch.complex64, dev)
+    psi = zero_state(n, (), torch.complex64, dev)
+    ms = _timed(lambda: prog.run(psi, inplace=True))
+    print(f"stage n={n} gates={gates} passes={prog.num_passes} {ms:.3f} ms")
+    return ms
+
+
+def gates(n: int = 24, kind: str = "H", k: int = 64) -> float:
+    from .circuits import gate_matrix
+    from .fusion import Circuit
+    dev = torch.device("cuda")
+
+    def q(bit):
+        return n - 1 - bit
+
+    c = Circuit(n)
+    for b in (6, 8, 10, 12, 14, 16, 18, 20):
+        c.h(q(b))
+    for i in range(k):
+        if kind == "H":
+            c.h(q(0))
+        elif kind == "X":
+            c.x(q(0))
+        elif kind == "RX":
+            c.append(gate_matrix("RX", 0.3 + i), [q(0)], "dense")
+        elif kind == "RZout":
+            c.append(gate_matrix("RZ", 0.3 + i), [q(5)], "diag")
+        else:
+            raise ValueError(f"unknown gate kind {kind}")
+    prog = c.compile(torch.complex64, dev, tile_qubits=12)
+    psi = torch.randn(2 ** n, dtype=torch.complex64, device=dev)
+    ms = _timed(lambda: prog.run(psi, inplace=True))
+    print(f"gates n={n} kind={kind} k={k} passes={prog.num_passes} "
+          f"{ms:.3f} ms")
+    return ms
+
+
+def adjoint(batch: int = 16, n: int = 20, layers: int = 12) -> float:
+    from .adjoint import PauliSum, expectation, hardware_efficient_ansatz
+    dev = torch.device("cuda")
+    pc = hardware_efficient_ansatz(n, layers)
+    H = PauliSum(n)
+    for i in range(n):
+        H.z(i)
+    for i in range(n - 1):
+        H.xx(i, i + 1, coeff=0.5)
+    g = torch.Generator(device=dev)
+    g.manual_seed(0)
+    params = torch.randn(batch, pc.num_params, generator=g, device=dev)
+
+    def step():
+        p = params.clone().requires_grad_()
+        expectation(pc, p, H).mean().backward()
+        return p.grad
+
+    ms = _timed(step)
+    print(f"adjoint n={n} layers={layers} batch={batch} {ms:.3f} ms")
+    return ms
+
+
+if __name__ == "__main__":
+    what, args = sys.argv[1], sys.argv[2:]
+    if what == "stage":
+        stage(*(int(a) for a in args))
+    elif what == "gates":
+        gates(int(args[0]) if args else 24, args[1] if len(args) > 1 else "H",
+              int(args[2]) if len(args) > 2 else 64)
+    elif what == "adjoint":
+        adjoint(*(int(a) for a in args))
+    else:
+        raise SystemExit(f"unknown workload {what}")
