@@ -357,7 +357,8 @@ typedef struct gbsv_adjoint_op {
  *   slot_scale[k] * Im <lam_s|P|psi_s>   (FP64, summed over the state's
  * tiles in index order) to grad[s * num_params + slot_param[k]].
  * slot_param / slot_scale are device arrays of num_slots entries; scratch
- * holds num_slots * num_states * 2^(n - tile_qubits) doubles. */
+ * holds num_slots * num_states * (2^(n - tile_qubits) + 2) doubles (tile
+ * partials, then the cos / sin of every rotation per state). */
 int gbsv_adjoint_stage(void* psi, void* lam, int dtype, int num_qubits,
                        int64_t num_states, int tile_qubits,
                        int contiguous_qubits, const int32_t* tile_positions,

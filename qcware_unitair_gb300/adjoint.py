@@ -529,7 +529,7 @@ def _backward_fused(pc, params, H, psi_L, saved, dtype):
         for entry in cache[key]:
             if entry[0] == "stage":
                 st = entry[1]
-                need = st["num_slots"] * tiles * 8
+                need = st["num_slots"] * (tiles + 2 * B) * 8
                 if need and (scratch is None or scratch.numel() < need):
                     scratch = torch.empty(need, dtype=torch.uint8, device=dev)
                 rc = L.gbsv_adjoint_stage(

@@ -334,6 +334,7 @@ struct AdjStageArgs {
   int params_f64;
   int64_t num_params;
   int num_slots;
+  const double* angles;  // (cos, sin) per (state, slot), from adjoint_angles
 };
 
 __device__ __forceinline__ int aswz(int l) {
@@ -404,6 +405,26 @@ __device__ __forceinline__ void adj_fixed(Cx<R>* S, int M, uint64_t base,
   }
 }
 
+// (cos, sin) of theta / 2 for every (state, rotation slot) of a stage, FP64
+__global__ void adjoint_angles_kernel(AdjStageArgs a, int64_t num_states,
+                                      double* out) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint64_t)num_states * a.num_ops) return;
+  const uint64_t s = i / a.num_ops;
+  const AdjOp& op = a.ops[i % a.num_ops];
+  if (op.kind != 0) return;
+  const double th =
+      op.scale *
+      (a.params_f64
+           ? static_cast<const double*>(a.params)[s * a.num_params + op.pidx]
+           : (double)static_cast<const float*>(
+                 a.params)[s * a.num_params + op.pidx]);
+  double sn, cs;
+  sincos(0.5 * th, &sn, &cs);
+  out[(s * a.num_slots + op.slot) * 2] = cs;
+  out[(s * a.num_slots + op.slot) * 2 + 1] = sn;
+}
+
 template <typename R>
 __global__ void __launch_bounds__(512, sizeof(R) == 4 ? 2 : 1)
     adjoint_stage_kernel(Cx<R>* psi, Cx<R>* lam, const Cx<R>* pool,
@@ -438,21 +459,11 @@ __global__ void __launch_bounds__(512, sizeof(R) == 4 ? 2 : 1)
     scale_sh.x = 1;
     scale_sh.y = 0;
   }
-  // cos and sin of every rotation of the stage, once per CTA: FP64 sincos
-  // on one thread per rotation instead of on every thread
+  // cos and sin of every rotation of the stage for this state, computed
+  // once per state by adjoint_angles_kernel
   R* csn = reinterpret_cast<R*>(wred + a.num_slots * (T >> 5));
-  for (int oi = tid; oi < a.num_ops; oi += T) {
-    const AdjOp& op = a.ops[oi];
-    if (op.kind != 0) continue;
-    const double th =
-        op.scale * (a.params_f64
-                        ? static_cast<const double*>(a.params)[s * a.num_params + op.pidx]
-                        : (double)static_cast<const float*>(a.params)[s * a.num_params + op.pidx]);
-    double sn, cs;
-    sincos(0.5 * th, &sn, &cs);
-    csn[2 * op.slot] = (R)cs;
-    csn[2 * op.slot + 1] = (R)sn;
-  }
+  for (int k = tid; k < 2 * a.num_slots; k += T)
+    csn[k] = (R)a.angles[s * 2 * a.num_slots + k];
   cp_async_wait_all();
   __syncthreads();
 
@@ -671,7 +682,10 @@ extern "C" int gbsv_adjoint_stage(
   const uint64_t tiles = (uint64_t)num_states * tiles_per_state;
   if (tiles > 0x7fffffffull)
     return set_error(GBSV_ERR_UNSUPPORTED, "too many tiles");
-  const size_t need = (size_t)num_slots * tiles * sizeof(double);
+  // scratch: per-tile partials, then (cos, sin) per (state, slot)
+  const size_t part_bytes = (size_t)num_slots * tiles * sizeof(double);
+  const size_t need =
+      part_bytes + (size_t)num_slots * num_states * 2 * sizeof(double);
   if (num_slots > 0 && (!scratch || scratch_bytes < need))
     return set_error(GBSV_ERR_SCRATCH, "adjoint stage needs %zu scratch bytes",
                      need);
@@ -688,6 +702,18 @@ extern "C" int gbsv_adjoint_stage(
                      "shared memory", num_slots, smem);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   double* partial = static_cast<double*>(scratch);
+  if (num_slots > 0) {
+    double* angles = reinterpret_cast<double*>(
+        static_cast<unsigned char*>(scratch) + part_bytes);
+    a.angles = angles;
+    const uint64_t items = (uint64_t)num_states * num_ops;
+    if (items > 0) {
+      adjoint_angles_kernel<<<(unsigned)((items + 255) / 256), 256, 0, st>>>(
+          a, num_states, angles);
+      const int rc = after_launch("adjoint_angles_kernel");
+      if (rc) return rc;
+    }
+  }
   if (dtype == GBSV_C64) {
     static bool attr = false;
     if (!attr) {
