@@ -917,6 +917,8 @@ __global__ void __launch_bounds__(RB >= 5 ? 256 : 512, 1)
   __shared__ uint64_t offh[NIT];
   __shared__ int16_t nv[TS_MAXG];   // values per gate, then their offsets
   __shared__ int8_t vp[TS_MAXG];    // value permutation of each gate
+  __shared__ int16_t grp[TS_MAXG];  // merged into the run headed by gate grp
+  __shared__ int8_t gm[TS_MAXG];    // bit 0: diagonal values, bit 1: head
   __shared__ int sh_total;
 
   const int T = blockDim.x;
@@ -944,7 +946,12 @@ __global__ void __launch_bounds__(RB >= 5 ? 256 : 512, 1)
   if (resident) {
     for (int gi = tid; gi < G; gi += T) {
       const FusedGate& g = gates[gi];
-      nv[gi] = (int16_t)fg_nvals(g.kind, g.nq);
+      // at least 4 values: a single-qubit diagonal that heads a merged
+      // run of single-qubit gates holds their 2x2 product
+      nv[gi] = (int16_t)max(fg_nvals(g.kind, g.nq), 4);
+      vp[gi] = 0;
+      grp[gi] = -1;
+      gm[gi] = 0;
     }
     __syncthreads();
     if (tid == 0) {
@@ -1004,6 +1011,7 @@ __global__ void __launch_bounds__(RB >= 5 ? 256 : 512, 1)
   const uint64_t offt = ts_tile_offset(a, tid * PER);
 
   // decode the resident gates and load values for state s
+  bool has_runs = false;
   auto load_values = [&](uint64_t s) {
     for (int gi = tid; gi < G; gi += T) {
       const FusedGate& g = gates[gi];
@@ -1023,6 +1031,35 @@ __global__ void __launch_bounds__(RB >= 5 ? 256 : 512, 1)
         const int F = vm & 3;
         for (int j = 0; j < k; ++j) mats[mo + j] = src[j ^ F];
       }
+    }
+    if (!has_runs) return;
+    __syncthreads();
+    // merged runs of single-qubit gates: the head holds M_last ... M_first
+    auto mat2 = [&](int gi, C* m) {
+      const C* x = mats + nv[gi];
+      if (gm[gi] & 1) {
+        m[0] = x[0];
+        m[1] = czero<C>();
+        m[2] = czero<C>();
+        m[3] = x[1];
+      } else {
+        for (int e = 0; e < 4; ++e) m[e] = x[e];
+      }
+    };
+    for (int h = tid; h < G; h += T) {
+      if (!(gm[h] & 2)) continue;
+      C acc[4], g2[4], r[4];
+      mat2(h, acc);
+      for (int j = h + 1; j < G; ++j) {
+        if (grp[j] != h) continue;
+        mat2(j, g2);
+        r[0] = cmad(g2[1], acc[2], cmul(g2[0], acc[0]));
+        r[1] = cmad(g2[1], acc[3], cmul(g2[0], acc[1]));
+        r[2] = cmad(g2[3], acc[2], cmul(g2[2], acc[0]));
+        r[3] = cmad(g2[3], acc[3], cmul(g2[2], acc[1]));
+        for (int e = 0; e < 4; ++e) acc[e] = r[e];
+      }
+      for (int e = 0; e < 4; ++e) mats[nv[h] + e] = acc[e];
     }
   };
   uint64_t loaded_s = t0 / tps;
@@ -1046,14 +1083,53 @@ __global__ void __launch_bounds__(RB >= 5 ? 256 : 512, 1)
       int perm[RB];
       for (int k = 0; k < RB; ++k) perm[k] = k;
       int flip = 0;
+      // open run of unconditioned single-qubit gates per physical bit:
+      // head gate and the position of its operation
+      int run_head[RB], run_pos[RB];
+      for (int k = 0; k < RB; ++k) run_head[k] = -1;
       for (int j = f; j < f + cnt; ++j) {
         TOp o = ts_decode<RB>(gates[j], nv[j], rb);
         vp[j] = 0;
+        grp[j] = -1;
+        gm[j] = 0;
         if (o.op == TOP_SCALAR) {
           ops[ps++] = o;
           continue;
         }
-        if (ts_relabel<RB>(o, perm, flip, vp[j])) ops[po++] = o;
+        if (!ts_relabel<RB>(o, perm, flip, vp[j])) continue;
+        const int op = o.op;
+        int b0 = -1, b1 = -1;  // physical register bits the op touches
+        bool single = false;   // an unconditioned single-qubit 2x2
+        if (op < TOP_DENSE2) {
+          b0 = op % 5;
+          single = op / 5 != TOP_SWAP1 / 5 && o.x == 0 && o.a == 0;
+        } else if (op < TOP_DIAG1) {
+          const int pp = (op - TOP_DENSE2) % 20;
+          b0 = pp >> 2;
+          b1 = (pp & 3) < b0 ? (pp & 3) : (pp & 3) + 1;
+        } else if (op < TOP_DIAG2) {
+          b0 = op - TOP_DIAG1;
+          single = o.nq == 1;
+          if (single) gm[j] = 1;
+        } else if (op < TOP_SCALAR) {
+          const int pp = op - TOP_DIAG2;
+          b0 = pp >> 2;
+          b1 = (pp & 3) < b0 ? (pp & 3) : (pp & 3) + 1;
+        }
+        if (single && run_head[b0] >= 0) {  // joins the open run
+          grp[j] = (int16_t)run_head[b0];
+          gm[run_head[b0]] |= 2;
+          ops[run_pos[b0]].op = (int16_t)(TOP_DENSE1 + b0);
+          has_runs = true;
+          continue;
+        }
+        if (b0 >= 0) run_head[b0] = -1;
+        if (b1 >= 0) run_head[b1] = -1;
+        if (single) {
+          run_head[b0] = j;
+          run_pos[b0] = po;
+        }
+        ops[po++] = o;
       }
       lay[li].count = po - f;
       lay[li].nscal = ns;
@@ -1065,7 +1141,7 @@ __global__ void __launch_bounds__(RB >= 5 ? 256 : 512, 1)
       }
       lay[li].cw = cw;
     }
-    __syncthreads();
+    has_runs = __syncthreads_or(has_runs);
     load_values(loaded_s);
   }
 

@@ -227,3 +227,31 @@ def test_x_and_swap_heavy_stages(oracle, dtype, tol, seed):
     out = prog.run(psi0.to(DEV))
     ref = oracle_run(oracle, circ, psi0.numpy())
     assert max_err(out.cpu().numpy(), ref) <= tol
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.complex64, 1e-5),
+                                       (torch.complex128, 1e-12)])
+def test_single_qubit_runs_merged(oracle, dtype, tol):
+    """Runs of single-qubit gates on one register bit (per-state rotations,
+    a diagonal, shared gates) are multiplied into one 2x2 per state."""
+    rng = np.random.default_rng(7)
+    n, B = 11, 3
+    circ = Circuit(n)
+    for _ in range(2):
+        for q in range(n):
+            for name in ("RX", "RY", "RZ"):
+                th = rng.uniform(0, 2 * np.pi, B)
+                mats = np.stack([gate_matrix(name, float(t)) for t in th])
+                circ.append(mats, [q], "diag" if name == "RZ" else "dense")
+            circ.t(q)
+            circ.h(q)
+        for q in range(n - 1):
+            circ.cnot(q, q + 1)
+    psi0 = random_states(n, (B,), dtype, seed=1)
+    prog = circ.compile(dtype, DEV, tile_qubits=11)
+    out = prog.run(psi0.to(DEV))
+    psi = psi0.numpy().astype(np.complex128)
+    for g in circ.gates:
+        psi = oracle.apply_operator(g.matrix.detach().cpu().numpy(),
+                                    list(g.qubits), psi)
+    assert max_err(out.cpu().numpy(), psi) <= tol
