@@ -460,17 +460,24 @@ def _plan_backward(pc: ParamCircuit, a: int, b: int, dtype, dev, m: int):
         c = min(c, m)
         order = list(range(c)) + sorted(p for p in tile if p >= c)
         local = {p: i for i, p in enumerate(order)}
-        recs, pool, slot_p, slot_s = [], [], [], []
+        G = len(item.gates)
+        recs = np.zeros(G, dtype=AD)  # filled by column: no per-record
+        kinds = np.zeros(G, np.int32)  # structured-array promotion
+        gens = np.zeros(G, np.int32)
+        bits = np.zeros(G, np.int32)
+        slots = np.zeros(G, np.int32)
+        pidxs = np.zeros(G, np.int32)
+        scales = np.zeros(G, np.float64)
+        pool, slot_p, slot_s = [], [], []
         pool_len = 0
-        for g in item.gates:
+        for i, g in enumerate(item.gates):
             op = index[id(g)]
-            r = np.zeros((), dtype=AD)
             if op[0] == "rot":
                 _, gen, q, pi, scale = op
                 pos = n - 1 - q
-                r["kind"], r["gen"] = 0, GEN[gen]
-                r["bit"] = local[pos] if pos in local else -1 - pos
-                r["slot"], r["pidx"], r["scale"] = len(slot_p), pi, scale
+                gens[i] = GEN[gen]
+                bits[i] = local[pos] if pos in local else -1 - pos
+                slots[i], pidxs[i], scales[i] = len(slot_p), pi, scale
                 slot_p.append(pi)
                 slot_s.append(scale)
             else:
@@ -479,13 +486,14 @@ def _plan_backward(pc: ParamCircuit, a: int, b: int, dtype, dev, m: int):
                 rec["mat"], rec["mat_bstride"] = pool_len, 0
                 pool.append(v)
                 pool_len += v.numel()
-                r["kind"] = 1
-                r["g"] = rec
-            recs.append(r)
+                kinds[i] = 1
+                recs["g"][i] = rec
+        recs["kind"], recs["gen"], recs["bit"] = kinds, gens, bits
+        recs["slot"], recs["pidx"], recs["scale"] = slots, pidxs, scales
         args = {
             "c": c, "positions": (ctypes_int32 * m)(*order),
-            "ops": _to_device(np.stack(recs).view(np.uint8), dev),
-            "num_ops": len(recs),
+            "ops": _to_device(recs.view(np.uint8), dev),
+            "num_ops": G,
             "pool": (torch.cat(pool) if pool else torch.zeros(1, dtype=dtype)
                      ).to(dev),
             "num_slots": len(slot_p),
