@@ -3,6 +3,7 @@
     python -m qcware_unitair_gb300.workloads stage 26          # random circuit
     python -m qcware_unitair_gb300.workloads gates 24 H 64     # one stage, 64 H
     python -m qcware_unitair_gb300.workloads adjoint 16        # 20q ansatz grad
+    python -m qcware_unitair_gb300.workloads serve 300         # server only
 
 Each runs its workload twice (a warm-up, then a CUDA-event-timed run) and
 prints one line; under a profiler, skip the first run's launches.
@@ -18,6 +19,11 @@ never a register bit), for the per-gate cost of the stage kernel.
 ``adjoint``: forward + adjoint backward of the 20-qubit, 12-layer
 hardware-efficient ansatz (RY, RZ per qubit, CZ ring) at the given batch,
 loss mean(<sum Z> + 0.5 <sum XX>).
+
+``serve``: the serving trace of the benchmark (Poisson 150 requests/s,
+10-22 qubits, depth 20-500, 1-64 states, 20% adjoint gradients) replayed
+once against the continuous-batching server after a 16-request warm-up,
+with the host time of the server's launch paths.
 """
 from __future__ import annotations
 
@@ -103,6 +109,44 @@ def adjoint(batch: int = 16, n: int = 20, layers: int = 12) -> float:
     return ms
 
 
+def serve(num: int = 300) -> float:
+    import collections
+    import time
+    from . import serve as S
+    dev = torch.device("cuda")
+    spent = collections.defaultdict(float)
+
+    def timed(obj, name, key):
+        f = getattr(obj, name)
+
+        def w(*a, **k):
+            t = time.perf_counter()
+            try:
+                return f(*a, **k)
+            finally:
+                spent[key] += time.perf_counter() - t
+        setattr(obj, name, w)
+        return f
+
+    warm = S.make_trace(16, rate=1000.0, seed=99, qubits=(10, 22),
+                        depth=(20, 100))
+    S.Server(dev).serve(warm)
+    saved = [(S.Server, "_launch_small",
+              timed(S.Server, "_launch_small", "small launches")),
+             (S.Server, "_launch_large",
+              timed(S.Server, "_launch_large", "large launches")),
+             (S, "_run_grad", timed(S, "_run_grad", "gradient requests"))]
+    try:
+        trace = S.make_trace(num, rate=150.0, seed=0, qubits=(10, 22))
+        res = S.summarize(S.Server(dev).serve(trace))
+    finally:
+        for obj, name, f in saved:
+            setattr(obj, name, f)
+    print(f"serve {res}; host seconds: "
+          + ", ".join(f"{k} {v:.3f}" for k, v in spent.items()))
+    return res["circuits_per_s"]
+
+
 if __name__ == "__main__":
     what, args = sys.argv[1], sys.argv[2:]
     if what == "stage":
@@ -112,5 +156,7 @@ if __name__ == "__main__":
               int(args[2]) if len(args) > 2 else 64)
     elif what == "adjoint":
         adjoint(*(int(a) for a in args))
+    elif what == "serve":
+        serve(*(int(a) for a in args))
     else:
         raise SystemExit(f"unknown workload {what}")
