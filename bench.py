@@ -436,6 +436,69 @@ def bench_c2(dev, layers=100):
             "broadcast_GBs": round(bc_bytes / (bc_ms / 1e3) / 1e9, 1)}
 
 
+# ------------------------------------------------- next-row operations ----
+def bench_next_rows(dev, n=30):
+    """The operations around the gate path on a 30-qubit complex64 state
+    (8 GiB, far above L2): qubit permutations (swap, permute, roll), the
+    phase-flip pass of multi_cz, multi-controlled X, apply_to_qubits with
+    one random single-qubit operator per qubit (fused), and sampling 2^20
+    outcomes.  Algorithmic bytes: a functional copy-like pass reads and
+    writes the state (16 B / amplitude); sampling reads it once (8 B)."""
+    import numpy as np
+    import torch
+    import qcware_unitair_gb300 as ug
+    from qcware_unitair_gb300.measurement import sample
+    N = 2 ** n
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    psi = torch.randn(N, dtype=torch.complex64, device=dev, generator=g)
+    psi /= torch.linalg.vector_norm(psi)
+    peak = peaks()[0]
+    rng = np.random.default_rng(3)
+    ops1 = torch.from_numpy(np.stack([
+        np.linalg.qr(rng.standard_normal((2, 2)) +
+                     1j * rng.standard_normal((2, 2)))[0]
+        for _ in range(n)])).to(dev, torch.complex64)
+    pairs = torch.tensor([[i, (i + 7) % n] for i in range(0, n, 3)],
+                         device=dev)
+    perm = list(reversed(range(n)))
+    cases = [
+        ("swap(0, 29)", lambda: ug.swap(psi, (0, n - 1)), 16),
+        ("permute_qubits(reversed)", lambda: ug.permute_qubits(perm, psi), 16),
+        ("roll_qubits(1)", lambda: ug.roll_qubits(psi, 1), 16),
+        ("multi_cz(10 pairs)", lambda: ug.multi_cz(pairs, psi), 16),
+        ("multi_controlled_x([0,1,2], 5)",
+         lambda: ug.multi_controlled_x(psi, [0, 1, 2], 5), 16),
+        ("apply_to_qubits(30 x 1q)",
+         lambda: ug.apply_to_qubits(list(ops1), list(range(n)), psi), None),
+        ("sample(2^20)", lambda: sample(psi, 1 << 20, seed=1), 8),
+    ]
+    out = {}
+    for name, fn, bpa in cases:
+        ms = _cuda_time(fn, 3)
+        row = {"ms": round(ms, 3)}
+        if bpa is not None:
+            gbs = bpa * N / (ms / 1e3) / 1e9
+            row.update({"GB_s": round(gbs, 1), "frac_of_peak": round(gbs / peak, 3)})
+        else:
+            prog_passes = None
+            try:
+                from qcware_unitair_gb300.fusion import Circuit
+                c = Circuit(n)
+                for q in range(n):
+                    c.append(ops1[q].cpu(), [q], "dense")
+                prog_passes = c.compile(torch.complex64, dev).num_passes
+            except Exception:  # informative only
+                pass
+            row.update({"passes": prog_passes,
+                        "GB_s_per_pass": round(16 * N * (prog_passes or 1) /
+                                               (ms / 1e3) / 1e9, 1)})
+        out[name] = row
+        torch.cuda.empty_cache()
+    return {"workload": f"{n}-qubit complex64 state (8 GiB), functional API",
+            "peak_GBs": peak, "ops": out}
+
+
 # ---------------------------------------------------------------- serving --
 def bench_serving(dev, num=300, rate=150.0, qubits=(10, 22)):
     """The serving trace (Poisson arrivals; qubits, depth 20-500 and 1-64
@@ -644,6 +707,7 @@ def run_gpu(args, ws, rank, local):
     if not args.no_extras:
         result["c0_12q_x64"] = bench_c0(dev)
         result["c2_16q_x4096"] = bench_c2(dev)
+        result["next_rows_30q"] = bench_next_rows(dev)
         result["adjoint"] = bench_adjoint(dev)
         result["serving"] = bench_serving(dev)
     if rank == 0 and not args.no_cpu_baseline:

@@ -20,26 +20,90 @@
 
 namespace gbsv {
 
+// A qubit permutation moves every amplitude; done as a tiled transpose so
+// that both the reads and the writes are runs of 2^c contiguous amplitudes.
+// Tile bits T (input positions): bits 0..c-1 (contiguous reads) plus the
+// input bits that land on output bits 0..c-1 (contiguous writes), topped up
+// with the lowest other bits to at least 11 (2048 amplitudes, 8 per
+// thread, so the per-tile index work is amortised).  A CTA reads a tile in input
+// order into shared memory and writes it back in output order; the other
+// bits pick the tile and move as a block.
+constexpr int PERM_MAX_TB = 11;
+
 struct PermArgs {
-  int n;
-  uint64_t total;
-  int src_pos[64];  // output bit position p reads input bit position src_pos[p]
+  int n, tb;
+  int tin[PERM_MAX_TB];   // input bit of tile-local bit j (j < c: bit j)
+  int wl[PERM_MAX_TB];    // output-local bit k: tile-local bit it comes from
+  int wp[PERM_MAX_TB];    // output-local bit k: output bit (k < c: bit k)
+  int rest_in[64];        // bits outside the tile, ascending
+  int rest_out[64];       // ... and where they land
+  uint64_t tiles_per_state, total_tiles;
 };
+
+template <typename R>
+__device__ __forceinline__ int perm_swz(int l) {
+  return sizeof(R) == 4 ? (l ^ ((l >> 4) & 15)) : (l ^ ((l >> 3) & 7));
+}
 
 template <typename R>
 __global__ void __launch_bounds__(256)
     permute_kernel(const Cx<R>* in, Cx<R>* out, PermArgs a) {
-  const uint64_t nmask = (uint64_t(1) << a.n) - 1;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-       i < a.total; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t o = i & nmask;
-    uint64_t src = 0;
-    for (int p = 0; p < a.n; ++p) src |= ((o >> p) & 1) << a.src_pos[p];
-    out[i] = in[(i - o) + src];
+  using C = Cx<R>;
+  __shared__ C S[1 << PERM_MAX_TB];
+  const int M = 1 << a.tb, T = blockDim.x, tid = threadIdx.x;
+  const int K = M / T;  // elements per thread per tile, <= 8
+  // per-thread offsets of its K tile elements, read and write side
+  uint64_t roff[8], woff[8];
+  int rl[8], wsm[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    roff[k] = woff[k] = 0;
+    rl[k] = wsm[k] = 0;
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    if (k >= K) break;
+    const int l = tid + k * T;
+    uint64_t ro = 0, wo = 0;
+    int ls = 0;
+    for (int j = 0; j < a.tb; ++j) {
+      if ((l >> j) & 1) {
+        ro |= uint64_t(1) << a.tin[j];
+        wo |= uint64_t(1) << a.wp[j];
+        ls |= 1 << a.wl[j];
+      }
+    }
+    roff[k] = ro;
+    rl[k] = perm_swz<R>(l);
+    woff[k] = wo;
+    wsm[k] = perm_swz<R>(ls);
+  }
+  const int nrest = a.n - a.tb;
+  for (uint64_t t = blockIdx.x; t < a.total_tiles; t += gridDim.x) {
+    const uint64_t s = t / a.tiles_per_state, r = t % a.tiles_per_state;
+    uint64_t bin = 0, bout = 0;
+    for (uint64_t x = r; x; x &= x - 1) {  // set bits only
+      const int j = __ffsll((long long)x) - 1;
+      bin |= uint64_t(1) << a.rest_in[j];
+      bout |= uint64_t(1) << a.rest_out[j];
+    }
+    (void)nrest;
+    const C* src = in + (s << a.n) + bin;
+    C* dst = out + (s << a.n) + bout;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (k < K) S[rl[k]] = __ldcs(src + roff[k]);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (k < K) __stcs(dst + woff[k], S[wsm[k]]);
+    __syncthreads();
   }
 }
 
-template <typename R>
+// V consecutive amplitudes per thread (32 bytes for complex64) so that
+// every access is a full sector
+template <typename R, int V>
 __global__ void __launch_bounds__(256)
     phase_flip_kernel(const Cx<R>* in, Cx<R>* out, uint64_t total, int n,
                       const uint64_t* masks, int num_masks) {
@@ -47,17 +111,32 @@ __global__ void __launch_bounds__(256)
   for (int k = threadIdx.x; k < num_masks; k += blockDim.x) sm[k] = masks[k];
   __syncthreads();
   const uint64_t nmask = (uint64_t(1) << n) - 1;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-       i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t x = i & nmask;
-    int parity = 0;
-    for (int k = 0; k < num_masks; ++k) parity ^= (x & sm[k]) == sm[k];
-    Cx<R> v = in[i];
-    if (parity) {
-      v.x = -v.x;
-      v.y = -v.y;
+  for (uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * V;
+       i < total; i += (uint64_t)gridDim.x * blockDim.x * V) {
+    Cx<R> v[V];
+    load_chunk<V>(in + i, v);
+    // the V amplitudes differ only in the low log2(V) index bits: a mask
+    // fires for amplitude e when its high part is set in the shared high
+    // bits and its low part is a subset of e
+    const uint64_t hi = i & nmask;
+    unsigned par = 0;  // bit e: parity of amplitude e
+    for (int k = 0; k < num_masks; ++k) {
+      const uint64_t m = sm[k];
+      const unsigned lo = (unsigned)(m & (V - 1));
+      if ((hi & (m & ~uint64_t(V - 1))) == (m & ~uint64_t(V - 1))) {
+        unsigned sub = 0;  // amplitudes e with lo a subset of e
+#pragma unroll
+        for (int e = 0; e < V; ++e) sub |= (((unsigned)e & lo) == lo) << e;
+        par ^= sub;
+      }
     }
-    out[i] = v;
+#pragma unroll
+    for (int e = 0; e < V; ++e)
+      if ((par >> e) & 1) {
+        v[e].x = -v[e].x;
+        v[e].y = -v[e].y;
+      }
+    store_chunk<V>(out + i, v);
   }
 }
 
@@ -79,63 +158,126 @@ __global__ void __launch_bounds__(256)
 }
 
 // ---- sampling ----------------------------------------------------------
+// Three tables over the state: SUB[i] = sum |psi|^2 over 32-amplitude group
+// i, SUMS[c] over 1024-amplitude chunk c (32 groups), CDF = inclusive
+// prefix of SUMS.  A sample binary-searches CDF for its chunk, then one warp
+// scans the chunk's 32 group sums and the chosen group's 32 amplitudes:
+// 32 + 32 reads instead of up to 1024.
 constexpr int CHUNK = 1024;
+constexpr int GROUP = 32;
 
+// one warp per chunk, lane l sums group l (32 contiguous amplitudes)
 template <typename R>
 __global__ void __launch_bounds__(256)
     chunk_sum_kernel(const Cx<R>* psi, uint64_t num_chunks, uint64_t dim,
-                     double* sums) {
-  const uint64_t c = blockIdx.x;
-  if (c >= num_chunks) return;
-  const Cx<R>* p = psi + c * CHUNK;
-  const uint64_t len = dim - c * CHUNK < (uint64_t)CHUNK ? dim - c * CHUNK
-                                                         : (uint64_t)CHUNK;
-  Acc<R> a;
-  for (int i = threadIdx.x; i < (int)len; i += blockDim.x) {
-    const Cx<R> v = p[i];
-    a.add_prod(v.x, v.x);
-    a.add_prod(v.y, v.y);
-  }
-  double acc = a.value();
-  __shared__ double sh[8];
+                     double* sums, double* subs) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+       c < num_chunks; c += nwarps) {
+    const uint64_t base = c * CHUNK + (uint64_t)lane * GROUP;
+    Acc<R> acc;
+    if (base + GROUP <= dim) {
+      constexpr int V = 32 / sizeof(Cx<R>);  // 32-byte pieces
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
-    sums[c] = t;
+      for (int j = 0; j < GROUP; j += V) {
+        Cx<R> v[V];
+        load_chunk<V>(psi + base + j, v);
+#pragma unroll
+        for (int e = 0; e < V; ++e) {
+          acc.add_prod(v[e].x, v[e].x);
+          acc.add_prod(v[e].y, v[e].y);
+        }
+      }
+    } else {
+      for (uint64_t i = base; i < dim && i < base + GROUP; ++i) {
+        const Cx<R> v = psi[i];
+        acc.add_prod(v.x, v.x);
+        acc.add_prod(v.y, v.y);
+      }
+    }
+    double g = acc.value();
+    subs[c * GROUP + lane] = g;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
+    if (lane == 0) sums[c] = g;
   }
 }
 
-// inclusive scan of num_chunks doubles by one block (sequential per thread
-// over a contiguous slice, then a scan of the slice totals)
-__global__ void __launch_bounds__(1024)
-    scan_kernel(const double* sums, double* cdf, uint64_t num_chunks) {
-  __shared__ double tot[1024];
-  const uint64_t per = (num_chunks + blockDim.x - 1) / blockDim.x;
-  const uint64_t lo = threadIdx.x * per;
-  uint64_t hi = lo + per;
-  if (hi > num_chunks) hi = num_chunks;
-  double acc = 0.0;
-  for (uint64_t i = lo; i < hi; ++i) acc += sums[i];
-  tot[threadIdx.x] = acc;
+// Block-wide exclusive scan of one double per thread (blockDim.x <= 1024);
+// returns the thread's exclusive prefix, *total the block's sum.
+__device__ __forceinline__ double block_exclusive_scan(double v,
+                                                       double* total) {
+  __shared__ double wsum[33];  // warp offsets, then the block total
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const double t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) wsum[w] = incl;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double run = 0.0;
-    for (int t = 0; t < (int)blockDim.x; ++t) {
-      const double v = tot[t];
-      tot[t] = run;
-      run += v;
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    double x = lane < nw ? wsum[lane] : 0.0;
+    double xi = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double t = __shfl_up_sync(0xffffffffu, xi, o);
+      if (lane >= o) xi += t;
     }
+    if (lane < nw) wsum[lane] = xi - x;  // exclusive warp offsets
+    if (lane == nw - 1) wsum[32] = xi;   // block total
   }
   __syncthreads();
-  double run = tot[threadIdx.x];
-  for (uint64_t i = lo; i < hi; ++i) {
-    run += sums[i];
-    cdf[i] = run;
+  const double r = wsum[w] + incl - v;
+  *total = wsum[32];
+  __syncthreads();
+  return r;
+}
+
+// Scan in three steps: per-block totals of seg-chunk segments, an exclusive
+// scan of the totals (one block), then each block's inclusive scan.
+__global__ void __launch_bounds__(1024)
+    scan_totals_kernel(const double* sums, uint64_t num_chunks, uint64_t seg,
+                       double* tot) {
+  const uint64_t lo = (uint64_t)blockIdx.x * seg;
+  const uint64_t per = seg / blockDim.x;
+  double acc = 0.0;
+  for (uint64_t k = 0; k < per; ++k) {
+    const uint64_t i = lo + threadIdx.x * per + k;
+    if (i < num_chunks) acc += sums[i];
   }
+  double total;
+  block_exclusive_scan(acc, &total);
+  if (threadIdx.x == 0) tot[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024)
+    scan_offsets_kernel(double* tot, int num_blocks) {
+  const double v = threadIdx.x < num_blocks ? tot[threadIdx.x] : 0.0;
+  double total;
+  const double ex = block_exclusive_scan(v, &total);
+  if (threadIdx.x < num_blocks) tot[threadIdx.x] = ex;
+}
+
+__global__ void __launch_bounds__(1024)
+    scan_blocks_kernel(const double* sums, uint64_t num_chunks, uint64_t seg,
+                       const double* offsets, double* cdf) {
+  const uint64_t lo = (uint64_t)blockIdx.x * seg;
+  const uint64_t per = seg / blockDim.x;
+  const uint64_t first = lo + threadIdx.x * per;
+  double acc = 0.0;
+  for (uint64_t k = 0; k < per; ++k)
+    if (first + k < num_chunks) acc += sums[first + k];
+  double total;
+  double run = offsets[blockIdx.x] + block_exclusive_scan(acc, &total);
+  for (uint64_t k = 0; k < per; ++k)
+    if (first + k < num_chunks) {
+      run += sums[first + k];
+      cdf[first + k] = run;
+    }
 }
 
 __device__ __forceinline__ uint64_t mix64(uint64_t z) {
@@ -148,48 +290,75 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
 
 template <typename R>
 __global__ void __launch_bounds__(256)
-    sample_kernel(const Cx<R>* psi, const double* cdf, uint64_t num_chunks,
-                  uint64_t dim, uint64_t num_samples, uint64_t seed,
-                  int64_t* out) {
+    sample_kernel(const Cx<R>* psi, const double* cdf, const double* subs,
+                  uint64_t num_chunks, uint64_t dim, uint64_t num_samples,
+                  uint64_t seed, int64_t* out) {
   const int lane = threadIdx.x & 31;
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   const double total = cdf[num_chunks - 1];
+  // every stride-th CDF value in shared memory: the first levels of the
+  // search stay on chip
+  constexpr int COARSE = 2048;
+  __shared__ double coarse[COARSE];
+  const uint64_t stride = (num_chunks + COARSE - 1) / COARSE;
+  const int ncoarse = (int)((num_chunks + stride - 1) / stride);
+  for (int i = threadIdx.x; i < ncoarse; i += blockDim.x) {
+    uint64_t e = (uint64_t)(i + 1) * stride;
+    if (e > num_chunks) e = num_chunks;
+    coarse[i] = cdf[e - 1];
+  }
+  __syncthreads();
   for (uint64_t sidx = warp; sidx < num_samples; sidx += nwarps) {
     const uint64_t h = mix64(seed ^ mix64(sidx));
     const double u = (double)(h >> 11) * (1.0 / 9007199254740992.0) * total;
-    // first chunk whose inclusive prefix exceeds u
-    uint64_t lo = 0, hi = num_chunks - 1;
+    // first chunk whose inclusive prefix exceeds u: coarse block, then
+    // within it
+    int clo = 0, chi = ncoarse - 1;
+    while (clo < chi) {
+      const int mid = (clo + chi) >> 1;
+      if (coarse[mid] > u) chi = mid; else clo = mid + 1;
+    }
+    uint64_t lo = (uint64_t)clo * stride;
+    uint64_t hi = (uint64_t)(clo + 1) * stride;
+    if (hi > num_chunks) hi = num_chunks;
+    hi -= 1;
     while (lo < hi) {
       const uint64_t mid = (lo + hi) >> 1;
       if (cdf[mid] > u) hi = mid; else lo = mid + 1;
     }
     double run = lo ? cdf[lo - 1] : 0.0;
     const uint64_t base = lo * CHUNK;
-    uint64_t len = dim - base;
-    if (len > CHUNK) len = CHUNK;
-    int64_t found = -1;
-    int64_t last_nonzero = -1;
-    for (uint64_t off = 0; off < len && found < 0; off += 32) {
-      double p = 0.0;
-      if (off + lane < len) {
-        const Cx<R> v = psi[base + off + lane];
-        p = (double)v.x * v.x + (double)v.y * v.y;
-      }
-      double incl = p;
+    // the chunk's 32 group sums, then the chosen group's 32 amplitudes
+    const double gs = subs[lo * GROUP + lane];
+    double gi = gs;
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const double t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += t;
-      }
-      const unsigned hit = __ballot_sync(0xffffffffu, p > 0.0 && run + incl > u);
-      const unsigned nz = __ballot_sync(0xffffffffu, p > 0.0);
-      if (nz) last_nonzero = (int64_t)(base + off) + 31 - __clz(nz);
-      if (hit) found = (int64_t)(base + off) + __ffs(hit) - 1;
-      run += __shfl_sync(0xffffffffu, incl, 31);
+    for (int o = 1; o < 32; o <<= 1) {
+      const double t = __shfl_up_sync(0xffffffffu, gi, o);
+      if (lane >= o) gi += t;
     }
+    unsigned hit = __ballot_sync(0xffffffffu, gs > 0.0 && run + gi > u);
+    const unsigned gnz = __ballot_sync(0xffffffffu, gs > 0.0);
     // rounding can leave u just above the chunk's own running sum
-    if (found < 0) found = last_nonzero >= 0 ? last_nonzero : (int64_t)base;
+    const int grp = hit ? __ffs(hit) - 1 : (gnz ? 31 - __clz(gnz) : 0);
+    run += __shfl_sync(0xffffffffu, gi - gs, grp);
+    const uint64_t gbase = base + (uint64_t)grp * GROUP;
+    double p = 0.0;
+    if (gbase + lane < dim) {
+      const Cx<R> v = psi[gbase + lane];
+      p = (double)v.x * v.x + (double)v.y * v.y;
+    }
+    double incl = p;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    hit = __ballot_sync(0xffffffffu, p > 0.0 && run + incl > u);
+    const unsigned nz = __ballot_sync(0xffffffffu, p > 0.0);
+    const int64_t found =
+        hit ? (int64_t)gbase + __ffs(hit) - 1
+            : (nz ? (int64_t)gbase + 31 - __clz(nz) : (int64_t)gbase);
     if (lane == 0) out[sidx] = found;
   }
 }
@@ -219,9 +388,7 @@ extern "C" int gbsv_permute_qubits(const void* in, void* out, int dtype,
     return set_error(GBSV_ERR_INVALID_ARG, "null pointer");
   if (in == out)
     return set_error(GBSV_ERR_INVALID_ARG, "permute_qubits is not in place");
-  PermArgs a{};
-  a.n = n;
-  a.total = (uint64_t)num_states << n;
+  int src_pos[64], dst_pos[64];
   uint64_t seen = 0;
   for (int j = 0; j < n; ++j) {
     const int q = perm[j];
@@ -230,14 +397,50 @@ extern "C" int gbsv_permute_qubits(const void* in, void* out, int dtype,
                        n);
     seen |= uint64_t(1) << q;
     // output qubit j (bit n-1-j) reads input qubit q (bit n-1-q)
-    a.src_pos[n - 1 - j] = n - 1 - q;
+    src_pos[n - 1 - j] = n - 1 - q;
+    dst_pos[n - 1 - q] = n - 1 - j;
   }
+  PermArgs a{};
+  a.n = n;
+  const int c = n < 5 ? n : 5;
+  uint64_t tmask = (uint64_t(1) << c) - 1;
+  for (int p = 0; p < c; ++p) tmask |= uint64_t(1) << src_pos[p];
+  for (int b = 0; b < n && __builtin_popcountll(tmask) < PERM_MAX_TB; ++b)
+    tmask |= uint64_t(1) << b;
+  a.tb = __builtin_popcountll(tmask);
+  // tile-local order: input bits 0..c-1 first, then the rest ascending
+  int nl = 0;
+  for (int b = 0; b < n; ++b)
+    if ((tmask >> b) & 1) a.tin[nl++] = b;
+  // output-local order: output positions of the tile bits, ascending
+  int outs[PERM_MAX_TB], no = 0;
+  for (int b = 0; b < n; ++b)
+    if ((tmask >> src_pos[b]) & 1) outs[no++] = b;
+  for (int k = 0; k < no; ++k) {
+    a.wp[k] = outs[k];
+    const int inb = src_pos[outs[k]];
+    for (int j = 0; j < a.tb; ++j)
+      if (a.tin[j] == inb) a.wl[k] = j;
+  }
+  int nr = 0;
+  for (int b = 0; b < n; ++b)
+    if (!((tmask >> b) & 1)) {
+      a.rest_in[nr] = b;
+      a.rest_out[nr] = dst_pos[b];
+      ++nr;
+    }
+  a.tiles_per_state = uint64_t(1) << (n - a.tb);
+  a.total_tiles = (uint64_t)num_states * a.tiles_per_state;
+  const int threads = (1 << a.tb) < 256 ? (1 << a.tb) : 256;  // K <= 8
+  uint64_t grid = a.total_tiles;
+  const uint64_t cap = (uint64_t)sm_count() * 8;
+  if (grid > cap) grid = cap;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (dtype == GBSV_C64)
-    permute_kernel<float><<<grid_for(a.total), 256, 0, st>>>(
+    permute_kernel<float><<<(unsigned)grid, threads, 0, st>>>(
         static_cast<const float2*>(in), static_cast<float2*>(out), a);
   else
-    permute_kernel<double><<<grid_for(a.total), 256, 0, st>>>(
+    permute_kernel<double><<<(unsigned)grid, threads, 0, st>>>(
         static_cast<const double2*>(in), static_cast<double2*>(out), a);
   return after_launch("permute_kernel");
 }
@@ -257,14 +460,29 @@ extern "C" int gbsv_phase_flip(const void* in, void* out, int dtype,
     return set_error(GBSV_ERR_INVALID_ARG, "null pointer");
   const uint64_t total = (uint64_t)num_states << num_qubits;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (dtype == GBSV_C64)
-    phase_flip_kernel<float><<<grid_for(total), 256, 0, st>>>(
-        static_cast<const float2*>(in), static_cast<float2*>(out), total,
-        num_qubits, static_cast<const uint64_t*>(masks), num_masks);
-  else
-    phase_flip_kernel<double><<<grid_for(total), 256, 0, st>>>(
-        static_cast<const double2*>(in), static_cast<double2*>(out), total,
-        num_qubits, static_cast<const uint64_t*>(masks), num_masks);
+  const uint64_t* mk = static_cast<const uint64_t*>(masks);
+  // 32-byte pieces need 4 (2) amplitudes per state and aligned buffers
+  const bool wide = num_qubits >= 2 && (uintptr_t)in % 32 == 0 &&
+                    (uintptr_t)out % 32 == 0;
+  if (dtype == GBSV_C64) {
+    auto i = static_cast<const float2*>(in);
+    auto o = static_cast<float2*>(out);
+    if (wide)
+      phase_flip_kernel<float, 4><<<grid_for(total / 4), 256, 0, st>>>(
+          i, o, total, num_qubits, mk, num_masks);
+    else
+      phase_flip_kernel<float, 1><<<grid_for(total), 256, 0, st>>>(
+          i, o, total, num_qubits, mk, num_masks);
+  } else {
+    auto i = static_cast<const double2*>(in);
+    auto o = static_cast<double2*>(out);
+    if (wide)
+      phase_flip_kernel<double, 2><<<grid_for(total / 2), 256, 0, st>>>(
+          i, o, total, num_qubits, mk, num_masks);
+    else
+      phase_flip_kernel<double, 1><<<grid_for(total), 256, 0, st>>>(
+          i, o, total, num_qubits, mk, num_masks);
+  }
   return after_launch("phase_flip_kernel");
 }
 
@@ -301,10 +519,16 @@ extern "C" int gbsv_multi_controlled_x(const void* in, void* out, int dtype,
   return after_launch("mcx_kernel");
 }
 
+// scratch: sums and cdf (one double per chunk each), group sums (32 per
+// chunk), and 1024 segment totals
+static uint64_t sample_chunks(int64_t dim) {
+  return ((uint64_t)dim + CHUNK - 1) / CHUNK;
+}
+
 extern "C" size_t gbsv_sample_scratch_bytes(int64_t dim) {
   if (dim <= 0) return 0;
-  const uint64_t chunks = ((uint64_t)dim + CHUNK - 1) / CHUNK;
-  return (size_t)chunks * 2 * sizeof(double);
+  const uint64_t chunks = sample_chunks(dim);
+  return (size_t)(chunks * (2 + GROUP) + 1024) * sizeof(double);
 }
 
 extern "C" int gbsv_sample(const void* state, int dtype, int64_t dim,
@@ -318,11 +542,11 @@ extern "C" int gbsv_sample(const void* state, int dtype, int64_t dim,
   if (num_samples == 0) return GBSV_OK;
   if (!state || !out_indices)
     return set_error(GBSV_ERR_INVALID_ARG, "null pointer");
-  const uint64_t chunks = ((uint64_t)dim + CHUNK - 1) / CHUNK;
+  const uint64_t chunks = sample_chunks(dim);
   if (dim % CHUNK != 0 && chunks > 1)
     return set_error(GBSV_ERR_INVALID_ARG, "dim must be a multiple of %d",
                      CHUNK);
-  const size_t need = chunks * 2 * sizeof(double);
+  const size_t need = gbsv_sample_scratch_bytes(dim);
   if (!scratch || scratch_bytes < need)
     return set_error(GBSV_ERR_SCRATCH, "sampling needs %zu scratch bytes",
                      need);
@@ -330,18 +554,35 @@ extern "C" int gbsv_sample(const void* state, int dtype, int64_t dim,
     return set_error(GBSV_ERR_UNSUPPORTED, "state too large");
   double* sums = static_cast<double*>(scratch);
   double* cdf = sums + chunks;
+  double* subs = cdf + chunks;
+  double* tot = subs + chunks * GROUP;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const int threads = dim < 256 ? 32 : 256;
-  if (dtype == GBSV_C64)
-    chunk_sum_kernel<float><<<(unsigned)chunks, threads, 0, st>>>(
-        static_cast<const float2*>(state), chunks, (uint64_t)dim, sums);
-  else
-    chunk_sum_kernel<double><<<(unsigned)chunks, threads, 0, st>>>(
-        static_cast<const double2*>(state), chunks, (uint64_t)dim, sums);
+  {
+    uint64_t blocks = (chunks * 32 + 255) / 256;
+    const uint64_t cap = (uint64_t)sm_count() * 16;
+    if (blocks > cap) blocks = cap;
+    if (dtype == GBSV_C64)
+      chunk_sum_kernel<float><<<(unsigned)blocks, 256, 0, st>>>(
+          static_cast<const float2*>(state), chunks, (uint64_t)dim, sums, subs);
+    else
+      chunk_sum_kernel<double><<<(unsigned)blocks, 256, 0, st>>>(
+          static_cast<const double2*>(state), chunks, (uint64_t)dim, sums,
+          subs);
+  }
   int rc = after_launch("chunk_sum_kernel");
   if (rc) return rc;
-  scan_kernel<<<1, 1024, 0, st>>>(sums, cdf, chunks);
-  rc = after_launch("scan_kernel");
+  // segments of seg chunks (a multiple of 1024), at most 1024 of them
+  uint64_t seg = 8192;
+  while ((chunks + seg - 1) / seg > 1024) seg *= 2;
+  const int nseg = (int)((chunks + seg - 1) / seg);
+  scan_totals_kernel<<<nseg, 1024, 0, st>>>(sums, chunks, seg, tot);
+  rc = after_launch("scan_totals_kernel");
+  if (rc) return rc;
+  scan_offsets_kernel<<<1, 1024, 0, st>>>(tot, nseg);
+  rc = after_launch("scan_offsets_kernel");
+  if (rc) return rc;
+  scan_blocks_kernel<<<nseg, 1024, 0, st>>>(sums, chunks, seg, tot, cdf);
+  rc = after_launch("scan_blocks_kernel");
   if (rc) return rc;
   const uint64_t warps = (uint64_t)num_samples;
   uint64_t blocks = (warps * 32 + 255) / 256;
@@ -349,11 +590,11 @@ extern "C" int gbsv_sample(const void* state, int dtype, int64_t dim,
   if (blocks > cap) blocks = cap;
   if (dtype == GBSV_C64)
     sample_kernel<float><<<(unsigned)blocks, 256, 0, st>>>(
-        static_cast<const float2*>(state), cdf, chunks, (uint64_t)dim,
+        static_cast<const float2*>(state), cdf, subs, chunks, (uint64_t)dim,
         (uint64_t)num_samples, seed, out_indices);
   else
     sample_kernel<double><<<(unsigned)blocks, 256, 0, st>>>(
-        static_cast<const double2*>(state), cdf, chunks, (uint64_t)dim,
+        static_cast<const double2*>(state), cdf, subs, chunks, (uint64_t)dim,
         (uint64_t)num_samples, seed, out_indices);
   return after_launch("sample_kernel");
 }

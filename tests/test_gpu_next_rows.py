@@ -107,3 +107,28 @@ def test_measure_large_state_chunks():
     assert set(np.unique(idx)) == {5, 2 ** n - 3}
     frac = np.mean(idx == 5)
     assert abs(frac - 0.36) < 0.01
+
+
+@pytest.mark.parametrize("n", [1, 3, 6, 12, 16])
+@pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
+def test_measure_distribution_sizes(n, dtype):
+    """Chunks of 1024 and groups of 32 amplitudes, partial groups for tiny
+    states, zero-probability groups, both precisions."""
+    rng = np.random.default_rng(n)
+    amps = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+    if n >= 6:
+        amps[32:64] = 0  # an empty group
+    amps /= np.linalg.norm(amps)
+    st = cu(amps.astype(dtype))
+    N = 200000
+    idx = ug.measurement.sample(st, N, seed=9).cpu().numpy()
+    assert idx.min() >= 0 and idx.max() < 2 ** n
+    p = np.abs(amps) ** 2
+    assert np.all(p[idx] > 0)
+    # binomial test on at most 1024 contiguous bins (enough samples per bin
+    # for the normal approximation)
+    nb = min(2 ** n, 1024)
+    pb = p.reshape(nb, -1).sum(axis=1)
+    freq = np.bincount(idx // (2 ** n // nb), minlength=nb) / N
+    sigma = np.sqrt(pb * (1 - pb) / N) + 1e-12
+    assert np.all(np.abs(freq - pb) <= 6 * sigma + 1e-9)
