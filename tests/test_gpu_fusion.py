@@ -255,3 +255,34 @@ def test_single_qubit_runs_merged(oracle, dtype, tol):
         psi = oracle.apply_operator(g.matrix.detach().cpu().numpy(),
                                     list(g.qubits), psi)
     assert max_err(out.cpu().numpy(), psi) <= tol
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.complex64, 1e-5),
+                                       (torch.complex128, 1e-12)])
+def test_stage_beyond_resident_limits(oracle, dtype, tol):
+    """A stage with more operations than stay resident per CTA (chunked
+    decode) and one with more layouts than the per-CTA table (per-layout
+    rebuild), both against the oracle."""
+    rng = np.random.default_rng(11)
+    n = 10
+    many_ops = Circuit(n)
+    for i in range(150):
+        a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+        if i % 3 == 0:
+            many_ops.append(gate_matrix("RZ", float(rng.uniform(0, 6))), [a],
+                            "diag")
+        elif i % 3 == 1:
+            many_ops.cz(a, b)
+        else:
+            many_ops.t(a)
+    many_ops.h(9)
+    many_ops.h(8)
+    many_layouts = Circuit(n)
+    for _ in range(120):
+        many_layouts.h(int(rng.integers(2, n)))
+    for circ in (many_ops, many_layouts):
+        psi0 = random_states(n, (2,), dtype, seed=4)
+        prog = circ.compile(dtype, DEV, tile_qubits=8)
+        out = prog.run(psi0.to(DEV))
+        ref = oracle_run(oracle, circ, psi0.numpy())
+        assert max_err(out.cpu().numpy(), ref) <= tol

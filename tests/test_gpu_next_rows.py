@@ -132,3 +132,21 @@ def test_measure_distribution_sizes(n, dtype):
     freq = np.bincount(idx // (2 ** n // nb), minlength=nb) / N
     sigma = np.sqrt(pb * (1 - pb) / N) + 1e-12
     assert np.all(np.abs(freq - pb) <= 6 * sigma + 1e-9)
+
+
+@pytest.mark.parametrize("n", [4, 9, 13, 15])
+@pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
+def test_random_permutations_tiled(n, dtype):
+    """permute_qubits against numpy's transpose of the tensor layout for
+    random permutations, batched, including ones that move the low bits."""
+    rng = np.random.default_rng(n)
+    B = 3
+    x = (rng.standard_normal((B, 2 ** n)) +
+         1j * rng.standard_normal((B, 2 ** n))).astype(dtype)
+    st = cu(x)
+    for _ in range(4):
+        perm = [int(p) for p in rng.permutation(n)]
+        ref = x.reshape((B,) + (2,) * n).transpose(
+            [0] + [1 + p for p in perm]).reshape(B, -1)
+        got = ug.permute_qubits(perm, st).cpu().numpy()
+        assert np.array_equal(got, ref)
