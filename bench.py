@@ -436,6 +436,55 @@ def bench_c2(dev, layers=100):
             "broadcast_GBs": round(bc_bytes / (bc_ms / 1e3) / 1e9, 1)}
 
 
+# ----------------------------------------------- the path's other rows ----
+def bench_path_rows(dev, n=30):
+    """apply_phase, the state reductions, apply_all_qubits and a 3-qubit
+    operator on a 30-qubit complex64 state (8 GiB).  Algorithmic bytes per
+    amplitude: phase 20 (angle 4 + read 8 + write 8), norm 8, inner product
+    16, |psi|^2 12 (read 8, write 4), diagonal expectation 12, a gate pass
+    16."""
+    import numpy as np
+    import torch
+    import qcware_unitair_gb300 as ug
+    N = 2 ** n
+    g = torch.Generator(device=dev)
+    g.manual_seed(7)
+    psi = torch.randn(N, dtype=torch.complex64, device=dev, generator=g)
+    psi /= torch.linalg.vector_norm(psi)
+    psi2 = torch.roll(psi, 1)
+    angles = torch.rand(N, device=dev, generator=g)
+    diag = torch.rand(N, device=dev, generator=g)
+    peak = peaks()[0]
+    h = torch.tensor([[1, 1], [1, -1]], dtype=torch.complex64,
+                     device=dev) / np.sqrt(2)
+    rng = np.random.default_rng(1)
+    u3 = np.linalg.qr(rng.standard_normal((8, 8)) +
+                      1j * rng.standard_normal((8, 8)))[0]
+    u3 = torch.from_numpy(u3).to(dev, torch.complex64)
+    cases = [
+        ("apply_phase(float32 angles)", lambda: ug.apply_phase(angles, psi),
+         20, 1),
+        ("norm_squared", lambda: ug.norm_squared(psi), 8, 1),
+        ("inner_product", lambda: ug.inner_product(psi, psi2), 16, 1),
+        ("abs_squared", lambda: ug.abs_squared(psi), 12, 1),
+        ("diag_expectation_value",
+         lambda: ug.diag_expectation_value(diag, psi), 12, 1),
+        ("apply_all_qubits(H)", lambda: ug.apply_all_qubits(h, psi), 16, n),
+        ("apply_operator(3 qubits)",
+         lambda: ug.apply_operator(u3, [3, 14, 27], psi), 16, 1),
+    ]
+    out = {}
+    for name, fn, bpa, passes in cases:
+        ms = _cuda_time(fn, 3)
+        gbs = bpa * N * passes / (ms / 1e3) / 1e9
+        out[name] = {"ms": round(ms, 3), "passes": passes,
+                     "GB_s": round(gbs, 1),
+                     "frac_of_peak": round(gbs / peak, 3)}
+        torch.cuda.empty_cache()
+    return {"workload": f"{n}-qubit complex64 state (8 GiB), functional API",
+            "peak_GBs": peak, "ops": out}
+
+
 # ------------------------------------------------- next-row operations ----
 def bench_next_rows(dev, n=30):
     """The operations around the gate path on a 30-qubit complex64 state
@@ -707,6 +756,7 @@ def run_gpu(args, ws, rank, local):
     if not args.no_extras:
         result["c0_12q_x64"] = bench_c0(dev)
         result["c2_16q_x4096"] = bench_c2(dev)
+        result["path_rows_30q"] = bench_path_rows(dev)
         result["next_rows_30q"] = bench_next_rows(dev)
         result["adjoint"] = bench_adjoint(dev)
         result["serving"] = bench_serving(dev)

@@ -180,6 +180,67 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// k = 3..5 target qubits: one thread per group of 2^k amplitudes.  The
+// thread reads its group once (consecutive threads take consecutive groups,
+// so every load instruction of a warp is contiguous when bit 0 is not a
+// target), multiplies by the matrix (in shared memory when one matrix
+// serves all states) and writes the group; in place is safe.
+template <typename R, int K>
+__global__ void __launch_bounds__(128)
+    dense_group_kernel(const Cx<R>* in, Cx<R>* out, const Cx<R>* ops,
+                       GenericArgs a) {
+  using C = Cx<R>;
+  constexpr int D = 1 << K;
+  __shared__ C msm[D * D];
+  __shared__ uint64_t offs[D];
+  __shared__ int spos[K];
+  const int tid = threadIdx.x;
+  if (tid < D) {
+    uint64_t o = 0;
+    for (int j = 0; j < K; ++j)
+      if ((tid >> (K - 1 - j)) & 1) o |= uint64_t(1) << a.pos[j];
+    offs[tid] = o;
+  }
+  if (tid == 0) {  // target positions ascending, for the zero insertion
+    int p[K];
+    for (int j = 0; j < K; ++j) p[j] = a.pos[j];
+    for (int i = 1; i < K; ++i)
+      for (int j = i; j > 0 && p[j - 1] > p[j]; --j) {
+        const int t = p[j];
+        p[j] = p[j - 1];
+        p[j - 1] = t;
+      }
+    for (int j = 0; j < K; ++j) spos[j] = p[j];
+  }
+  const bool shared_op = a.op_stride == 0;
+  if (shared_op)
+    for (int i = tid; i < D * D; i += blockDim.x) msm[i] = ops[i];
+  __syncthreads();
+  const int n = a.n;
+  const uint64_t gps = uint64_t(1) << (n - K);  // groups per state
+  const uint64_t total = (a.total >> n) * gps;
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + tid; g < total;
+       g += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t s = g / gps;
+    uint64_t base = g % gps;
+#pragma unroll
+    for (int j = 0; j < K; ++j) base = insert_zero(base, spos[j]);
+    const C* src = in + s * a.in_stride + base;
+    C* dst = out + (s << n) + base;
+    C x[D];
+#pragma unroll
+    for (int b = 0; b < D; ++b) x[b] = src[offs[b]];
+    const C* m = shared_op ? msm : ops + s * a.op_stride;
+#pragma unroll 4
+    for (int r = 0; r < D; ++r) {
+      C acc = czero<C>();
+#pragma unroll
+      for (int b = 0; b < D; ++b) acc = cmad(m[r * D + b], x[b], acc);
+      dst[offs[r]] = acc;
+    }
+  }
+}
+
 // ------------------------------------------------------------ dispatch --
 template <typename R, int V, int K, int NH, int RB0, int RB1>
 static int launch_chunk(const void* in, void* out, const void* ops,
@@ -290,6 +351,28 @@ static int apply_generic(const void* in, void* out, int dtype, int n,
   for (int j = 0; j < k; ++j) {
     a.pos[j] = pos[j];
     a.tmask |= uint64_t(1) << pos[j];
+  }
+  const int kmax_group = dtype == GBSV_C64 ? 5 : 4;
+  if (k >= 3 && k <= kmax_group && n >= k) {
+    uint64_t groups = a.total >> k;
+    uint64_t gb = (groups + 127) / 128;
+    const uint64_t gcap = (uint64_t)sm_count() * 32;
+    if (gb > gcap) gb = gcap;
+    if (gb < 1) gb = 1;
+#define GBSV_GROUP(R, KK)                                                  \
+  dense_group_kernel<R, KK><<<(unsigned)gb, 128, 0, st>>>(                \
+      static_cast<const Cx<R>*>(in), static_cast<Cx<R>*>(out),             \
+      static_cast<const Cx<R>*>(ops), a)
+    if (dtype == GBSV_C64) {
+      if (k == 3) GBSV_GROUP(float, 3);
+      else if (k == 4) GBSV_GROUP(float, 4);
+      else GBSV_GROUP(float, 5);
+    } else {
+      if (k == 3) GBSV_GROUP(double, 3);
+      else GBSV_GROUP(double, 4);
+    }
+#undef GBSV_GROUP
+    return after_launch("dense_group_kernel");
   }
   const size_t smem = sizeof(uint64_t) << k;
   uint64_t blocks = (a.total + 255) / 256;

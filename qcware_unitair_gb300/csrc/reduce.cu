@@ -40,7 +40,7 @@ struct Plan {
 static Plan make_plan(int64_t rows, int64_t dim) {
   Plan p{1, dim};
   if (rows <= 0 || dim <= 0) return p;
-  const int64_t want_blocks = (int64_t)sm_count() * 4;
+  const int64_t want_blocks = (int64_t)sm_count() * 16;
   const int64_t min_len = 8192;
   if (rows >= want_blocks || dim <= min_len) return p;
   int64_t parts = (want_blocks + rows - 1) / rows;
@@ -116,7 +116,18 @@ __global__ void __launch_bounds__(RED_THREADS)
   if (hi > dim) hi = dim;
   const Cx<R>* p = psi + row * dim;
   Acc<R> acc;
-  for (int64_t i = lo + threadIdx.x; i < hi; i += RED_THREADS) {
+  int64_t i = lo + threadIdx.x;
+  for (; i + 3 * RED_THREADS < hi; i += 4 * RED_THREADS) {
+    Cx<R> v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = __ldcs(p + i + k * RED_THREADS);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      acc.add_prod(v[k].x, v[k].x);
+      acc.add_prod(v[k].y, v[k].y);
+    }
+  }
+  for (; i < hi; i += RED_THREADS) {
     const Cx<R> v = __ldcs(p + i);
     acc.add_prod(v.x, v.x);
     acc.add_prod(v.y, v.y);
@@ -174,15 +185,26 @@ __global__ void __launch_bounds__(RED_THREADS)
   int64_t hi = lo + ra.part_len;
   if (hi > ra.dim) hi = ra.dim;
   Acc<R> x, y;
-  for (int64_t i = lo + threadIdx.x; i < hi; i += RED_THREADS) {
-    const Cx<R> u = a[oa + i * ra.ia];
-    const Cx<R> v = b[ob + i * ra.ib];
-    // conj(u) * v
+  auto step = [&](const Cx<R>& u, const Cx<R>& v) {  // += conj(u) * v
     x.add_prod(u.x, v.x);
     x.add_prod(u.y, v.y);
     y.add_prod(u.x, v.y);
     y.add_prod(-u.y, v.x);
+  };
+  int64_t i = lo + threadIdx.x;
+  // four elements of each input in flight per thread
+  for (; i + 3 * RED_THREADS < hi; i += 4 * RED_THREADS) {
+    Cx<R> u[4], v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      u[k] = __ldcs(a + oa + (i + k * RED_THREADS) * ra.ia);
+      v[k] = __ldcs(b + ob + (i + k * RED_THREADS) * ra.ib);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) step(u[k], v[k]);
   }
+  for (; i < hi; i += RED_THREADS)
+    step(a[oa + i * ra.ia], b[ob + i * ra.ib]);
   const double2 s = block_sum2(x.value(), y.value());
   if (threadIdx.x == 0) {
     if (ra.parts == 1) {
@@ -212,13 +234,25 @@ __global__ void __launch_bounds__(RED_THREADS)
   // diag * |psi|^2 in the state's precision (FP64 when either input is)
   using W = typename std::conditional<(sizeof(RD) > sizeof(R)), RD, R>::type;
   Acc<W> acc;
-  for (int64_t i = lo + threadIdx.x; i < hi; i += RED_THREADS) {
-    const W w = (W)d[oa + i * ra.ia];
-    const Cx<R> v = psi[ob + i * ra.ib];
+  auto step = [&](const RD dv, const Cx<R>& v) {
+    const W w = (W)dv;
     const W x = (W)v.x, y = (W)v.y;
     acc.add_prod(w * x, x);
     acc.add_prod(w * y, y);
+  };
+  int64_t i = lo + threadIdx.x;
+  for (; i + 3 * RED_THREADS < hi; i += 4 * RED_THREADS) {
+    RD dv[4];
+    Cx<R> v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      dv[k] = __ldcs(d + oa + (i + k * RED_THREADS) * ra.ia);
+      v[k] = __ldcs(psi + ob + (i + k * RED_THREADS) * ra.ib);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) step(dv[k], v[k]);
   }
+  for (; i < hi; i += RED_THREADS) step(d[oa + i * ra.ia], psi[ob + i * ra.ib]);
   const double2 s = block_sum2(acc.value(), 0.0);
   if (threadIdx.x == 0) {
     if (ra.parts == 1) {
@@ -236,8 +270,18 @@ __global__ void __launch_bounds__(RED_THREADS)
 template <typename R>
 __global__ void __launch_bounds__(256)
     abs2_kernel(const Cx<R>* psi, R* out, uint64_t count) {
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
-       i += (uint64_t)gridDim.x * blockDim.x) {
+  // four amplitudes per thread and step (several loads in flight)
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < count; i += 4 * stride) {
+    Cx<R> v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = __ldcs(psi + i + k * stride);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      __stcs(out + i + k * stride, v[k].x * v[k].x + v[k].y * v[k].y);
+  }
+  for (; i < count; i += stride) {
     const Cx<R> v = __ldcs(psi + i);
     __stcs(out + i, v.x * v.x + v.y * v.y);
   }

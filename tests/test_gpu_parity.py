@@ -305,3 +305,32 @@ def test_launch_counter_counts_kernels():
     ug.apply_operator(ug.gates.hadamard(device=DEV), [2], st)
     ug.norm_squared(st)
     assert _lib.launch_count() - before == 2
+
+
+@pytest.mark.parametrize("k", [3, 4, 5])
+@pytest.mark.parametrize("dtype,tol", [(torch.complex64, 2e-6),
+                                       (torch.complex128, 1e-13)])
+def test_wide_operators_group_kernel(oracle, k, dtype, tol):
+    """3- to 5-qubit operators (one thread per group of 2^k amplitudes):
+    shared and per-state matrices, target 0 among the targets or not, and
+    in place, against the complex128 oracle."""
+    import qcware_unitair_gb300 as ug
+    rng = np.random.default_rng(40 + k)
+    n, B = 9, 3
+    psi = (rng.standard_normal((B, 2 ** n)) +
+           1j * rng.standard_normal((B, 2 ** n)))
+    for qubits in ([int(q) for q in rng.choice(n, k, replace=False)],
+                   [n - 1] + [int(q) for q in rng.choice(n - 1, k - 1,
+                                                        replace=False)]):
+        for batched in (False, True):
+            shape = (B, 2 ** k, 2 ** k) if batched else (2 ** k, 2 ** k)
+            op = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+            st = torch.from_numpy(psi).to(DEV, dtype)
+            got = ug.apply_operator(torch.from_numpy(op).to(DEV, dtype),
+                                    qubits, st).cpu().numpy()
+            ref = oracle.apply_operator(op, qubits, psi)
+            assert np.abs(got - ref).max() <= tol * np.abs(ref).max()
+            ug.apply_operator_(torch.from_numpy(op).to(DEV, dtype), qubits,
+                               st)
+            assert np.abs(st.cpu().numpy() - ref).max() <= (
+                tol * np.abs(ref).max())
