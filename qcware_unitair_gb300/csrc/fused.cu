@@ -361,7 +361,8 @@ extern "C" int gbsv_run_stage(const void* state_in, void* state_out, int dtype,
 // gate costs one uniform jump-table dispatch plus its arithmetic.
 //
 // Shared-memory addresses use an XOR-linear swizzle (complex64: bits 1-3 of
-// the amplitude index ^= bits 4-6; complex128: bits 0-2 ^= bits 3-5).
+// the amplitude index ^= bits 4-6, bit 0 stays so that 16-byte pieces stay
+// whole for the tile copies; complex128: bits 0-2 ^= bits 3-5).
 // Because it is linear and a thread's offset bits are disjoint from its
 // register bits, address(register i) = swz(thread offset) ^ swz(register
 // offset i), both read from per-layout tables.
@@ -890,6 +891,55 @@ __device__ __forceinline__ void ts_run(Cx<R>* v, const TOp* ops,
   }
 }
 
+// Which tile bit each thread-index bit stands for in a layout.  Shared
+// memory is read and written at (thread bits | register bits), swizzled; a
+// half-warp's 16 lanes (complex64, 8-byte accesses; a quarter-warp of 8
+// lanes for complex128) hit distinct banks exactly when the swizzled
+// low-address images of their lane bits are linearly independent over
+// GF(2).  So the lowest thread-index bits take, in ascending order, the
+// non-register tile bits that raise that rank, then the rest ascending.
+// The order is packed 4 bits per thread-index bit (at most 14 - RB <= 11).
+__device__ __forceinline__ int ts_order_get(uint64_t ord, int j) {
+  return (int)((ord >> (4 * j)) & 15);
+}
+
+template <typename R>
+__device__ uint64_t ts_thread_bit_order(int rbmask, int m) {
+  constexpr int BANK_BITS = sizeof(R) == 4 ? 4 : 3;
+  // image of tile bit b in the low BANK_BITS address bits after swz_amp
+  auto image = [](int b) {
+    const int a = swz_amp<R>(1 << b);
+    return a & ((1 << BANK_BITS) - 1);
+  };
+  int lead[BANK_BITS];  // basis vector whose highest set bit is h, or 0
+  for (int h = 0; h < BANK_BITS; ++h) lead[h] = 0;
+  int nb = 0;
+  uint64_t ord = 0;
+  int taken = 0, j = 0;
+  for (int b = 0; b < m && nb < BANK_BITS; ++b) {
+    if ((rbmask >> b) & 1) continue;
+    int v = image(b);
+    bool added = false;
+    for (int h = BANK_BITS - 1; h >= 0 && v; --h) {
+      if (!((v >> h) & 1)) continue;
+      if (lead[h] == 0) {
+        lead[h] = v;
+        added = true;
+        break;
+      }
+      v ^= lead[h];
+    }
+    if (!added) continue;
+    ++nb;
+    ord |= (uint64_t)b << (4 * j++);
+    taken |= 1 << b;
+  }
+  for (int b = 0; b < m; ++b)
+    if (!((rbmask >> b) & 1) && !((taken >> b) & 1))
+      ord |= (uint64_t)b << (4 * j++);
+  return ord;
+}
+
 // Offset (in amplitudes, within the state) of tile amplitude l: the low c
 // bits are contiguous, bit c + j of l lands on global position hpos[j].
 __device__ __forceinline__ uint64_t ts_tile_offset(const Stage2Args& a,
@@ -979,10 +1029,10 @@ __global__ void __launch_bounds__(RB >= 5 ? 256 : 512, 1)
     for (int k = 0; k < RB; ++k) rbmask |= 1 << ly.rb[k];
     if (e < 48) {
       const int tbits = e < 32 ? e : (e - 32) << 5;
+      const uint64_t ord = ts_thread_bit_order<R>(rbmask, a.m);
       int tb = 0, t = tbits;
-      for (int bit = 0; bit < a.m && t; ++bit) {
-        if ((rbmask >> bit) & 1) continue;
-        tb |= (t & 1) << bit;
+      for (int j = 0; j < a.m - RB && t; ++j) {
+        tb |= (t & 1) << ts_order_get(ord, j);
         t >>= 1;
       }
       if (e < 32) {
