@@ -181,8 +181,20 @@ __global__ void __launch_bounds__(256)
       constexpr int V = 32 / sizeof(Cx<R>);  // 32-byte pieces
 #pragma unroll
       for (int j = 0; j < GROUP; j += V) {
+        // cached loads: the lanes read 256 B apart, so both halves of a
+        // sector are read by one lane in consecutive loads
         Cx<R> v[V];
-        load_chunk<V>(psi + base + j, v);
+        if constexpr (sizeof(R) == 4) {
+          const float4 q0 = reinterpret_cast<const float4*>(psi + base + j)[0];
+          const float4 q1 = reinterpret_cast<const float4*>(psi + base + j)[1];
+          v[0] = make_float2(q0.x, q0.y);
+          v[1] = make_float2(q0.z, q0.w);
+          v[2] = make_float2(q1.x, q1.y);
+          v[3] = make_float2(q1.z, q1.w);
+        } else {
+#pragma unroll
+          for (int e = 0; e < V; ++e) v[e] = psi[base + j + e];
+        }
 #pragma unroll
         for (int e = 0; e < V; ++e) {
           acc.add_prod(v[e].x, v[e].x);
@@ -327,35 +339,37 @@ __global__ void __launch_bounds__(256)
       const uint64_t mid = (lo + hi) >> 1;
       if (cdf[mid] > u) hi = mid; else lo = mid + 1;
     }
-    double run = lo ? cdf[lo - 1] : 0.0;
+    const double run = lo ? cdf[lo - 1] : 0.0;
     const uint64_t base = lo * CHUNK;
+    // the rest of u inside the chunk; FP32 from here (a chunk's share only)
+    float rem = (float)(u - run);
     // the chunk's 32 group sums, then the chosen group's 32 amplitudes
-    const double gs = subs[lo * GROUP + lane];
-    double gi = gs;
+    const float gs = (float)subs[lo * GROUP + lane];
+    float gi = gs;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const double t = __shfl_up_sync(0xffffffffu, gi, o);
+      const float t = __shfl_up_sync(0xffffffffu, gi, o);
       if (lane >= o) gi += t;
     }
-    unsigned hit = __ballot_sync(0xffffffffu, gs > 0.0 && run + gi > u);
-    const unsigned gnz = __ballot_sync(0xffffffffu, gs > 0.0);
+    unsigned hit = __ballot_sync(0xffffffffu, gs > 0.f && gi > rem);
+    const unsigned gnz = __ballot_sync(0xffffffffu, gs > 0.f);
     // rounding can leave u just above the chunk's own running sum
     const int grp = hit ? __ffs(hit) - 1 : (gnz ? 31 - __clz(gnz) : 0);
-    run += __shfl_sync(0xffffffffu, gi - gs, grp);
+    rem -= __shfl_sync(0xffffffffu, gi - gs, grp);
     const uint64_t gbase = base + (uint64_t)grp * GROUP;
-    double p = 0.0;
+    float p = 0.f;
     if (gbase + lane < dim) {
       const Cx<R> v = psi[gbase + lane];
-      p = (double)v.x * v.x + (double)v.y * v.y;
+      p = (float)((R)v.x * v.x + (R)v.y * v.y);
     }
-    double incl = p;
+    float incl = p;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const double t = __shfl_up_sync(0xffffffffu, incl, o);
+      const float t = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += t;
     }
-    hit = __ballot_sync(0xffffffffu, p > 0.0 && run + incl > u);
-    const unsigned nz = __ballot_sync(0xffffffffu, p > 0.0);
+    hit = __ballot_sync(0xffffffffu, p > 0.f && incl > rem);
+    const unsigned nz = __ballot_sync(0xffffffffu, p > 0.f);
     const int64_t found =
         hit ? (int64_t)gbase + __ffs(hit) - 1
             : (nz ? (int64_t)gbase + 31 - __clz(nz) : (int64_t)gbase);
