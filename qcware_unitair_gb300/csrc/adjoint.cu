@@ -405,6 +405,62 @@ __device__ __forceinline__ void adj_fixed(Cx<R>* S, int M, uint64_t base,
   }
 }
 
+// One rotation's step on one amplitude pair (x0, x1 of psi, l0, l1 of
+// lambda along the rotation's bit): adds Im <lambda|P|psi> restricted to the
+// pair to g, then uncomputes both with U^dag = cos I + i sin P.
+template <typename C, typename R>
+__device__ __forceinline__ void adj_pair(int gen, R c, R sr, C& x0, C& x1,
+                                         C& l0, C& l1, R& g) {
+  C q0, q1, m0, m1;
+  if (gen == 0) {  // X: conj(l0) x1 + conj(l1) x0
+    g = fma(l0.x, x1.y, g);
+    g = fma(-l0.y, x1.x, g);
+    g = fma(l1.x, x0.y, g);
+    g = fma(-l1.y, x0.x, g);
+    q0.x = c * x0.x - sr * x1.y; q0.y = c * x0.y + sr * x1.x;
+    q1.x = c * x1.x - sr * x0.y; q1.y = c * x1.y + sr * x0.x;
+    m0.x = c * l0.x - sr * l1.y; m0.y = c * l0.y + sr * l1.x;
+    m1.x = c * l1.x - sr * l0.y; m1.y = c * l1.y + sr * l0.x;
+  } else if (gen == 1) {  // Y
+    g = fma(l1.x, x0.x, g);
+    g = fma(l1.y, x0.y, g);
+    g = fma(-l0.x, x1.x, g);
+    g = fma(-l0.y, x1.y, g);
+    q0.x = c * x0.x + sr * x1.x; q0.y = c * x0.y + sr * x1.y;
+    q1.x = c * x1.x - sr * x0.x; q1.y = c * x1.y - sr * x0.y;
+    m0.x = c * l0.x + sr * l1.x; m0.y = c * l0.y + sr * l1.y;
+    m1.x = c * l1.x - sr * l0.x; m1.y = c * l1.y - sr * l0.y;
+  } else {  // Z
+    g = fma(l0.x, x0.y, g);
+    g = fma(-l0.y, x0.x, g);
+    g = fma(-l1.x, x1.y, g);
+    g = fma(l1.y, x1.x, g);
+    q0.x = c * x0.x - sr * x0.y; q0.y = c * x0.y + sr * x0.x;
+    q1.x = c * x1.x + sr * x1.y; q1.y = c * x1.y - sr * x1.x;
+    m0.x = c * l0.x - sr * l0.y; m0.y = c * l0.y + sr * l0.x;
+    m1.x = c * l1.x + sr * l1.y; m1.y = c * l1.y - sr * l1.x;
+  }
+  x0 = q0;
+  x1 = q1;
+  l0 = m0;
+  l1 = m1;
+}
+
+// Warp partial of a rotation's gradient into wred[slot * warps + warp].
+template <typename R>
+__device__ __forceinline__ void adj_warp_partial(R gsum, double* wred,
+                                                 int slot, int T, int tid) {
+  if constexpr (sizeof(R) == 4) {
+    float hi = gsum, lo = 0.f;
+    warp_sum_pair(hi, lo);
+    if ((tid & 31) == 0)
+      wred[slot * (T >> 5) + (tid >> 5)] = (double)hi + (double)lo;
+  } else {
+    const double gr = warp_sum_adj(gsum);
+    if ((tid & 31) == 0) wred[slot * (T >> 5) + (tid >> 5)] = gr;
+  }
+}
+
 // (cos, sin) of theta / 2 for every (state, rotation slot) of a stage, FP64
 __global__ void adjoint_angles_kernel(AdjStageArgs a, int64_t num_states,
                                       double* out) {
@@ -495,6 +551,11 @@ __global__ void __launch_bounds__(512, sizeof(R) == 4 ? 2 : 1)
     // a thread sums only its few pairs of the tile (plain FMA); precision
     // is kept where the sums grow: across lanes, warps and tiles
     R gsum = 0;
+    // the next op, when it is a rotation on a tile bit, shares this sweep
+    const AdjOp* op2 = nullptr;
+    if (op.bit >= 0 && oi + 1 < a.num_ops && a.ops[oi + 1].kind == 0 &&
+        a.ops[oi + 1].bit >= 0)
+      op2 = &a.ops[oi + 1];
     if (op.bit < 0) {
       // Z on a bit outside the tile: the tile sits at z = +/-1
       const int zb = (int)((base >> (-1 - op.bit)) & 1);
@@ -513,58 +574,73 @@ __global__ void __launch_bounds__(512, sizeof(R) == 4 ? 2 : 1)
         scale_sh = cmul(scale_sh, f);
         // a per-tile factor multiplies psi and lambda alike
       }
-    } else {
+    } else if (op2 == nullptr) {
       const int b = op.bit;
       for (int j = tid; j < (M >> 1); j += T) {
         const int i0 = (int)insert_zero((uint64_t)j, b);
         const int i1 = i0 | (1 << b);
         const int p0 = PER == 2 ? aswz(i0) : i0, p1 = PER == 2 ? aswz(i1) : i1;
-        const C x0 = SP[p0], x1 = SP[p1], l0 = SL[p0], l1 = SL[p1];
-        C q0, q1, m0, m1;
-        if (op.gen == 0) {
-          gsum = fma(l0.x, x1.y, gsum);
-          gsum = fma(-l0.y, x1.x, gsum);
-          gsum = fma(l1.x, x0.y, gsum);
-          gsum = fma(-l1.y, x0.x, gsum);
-          q0.x = c * x0.x - sr * x1.y; q0.y = c * x0.y + sr * x1.x;
-          q1.x = c * x1.x - sr * x0.y; q1.y = c * x1.y + sr * x0.x;
-          m0.x = c * l0.x - sr * l1.y; m0.y = c * l0.y + sr * l1.x;
-          m1.x = c * l1.x - sr * l0.y; m1.y = c * l1.y + sr * l0.x;
-        } else if (op.gen == 1) {
-          gsum = fma(l1.x, x0.x, gsum);
-          gsum = fma(l1.y, x0.y, gsum);
-          gsum = fma(-l0.x, x1.x, gsum);
-          gsum = fma(-l0.y, x1.y, gsum);
-          q0.x = c * x0.x + sr * x1.x; q0.y = c * x0.y + sr * x1.y;
-          q1.x = c * x1.x - sr * x0.x; q1.y = c * x1.y - sr * x0.y;
-          m0.x = c * l0.x + sr * l1.x; m0.y = c * l0.y + sr * l1.y;
-          m1.x = c * l1.x - sr * l0.x; m1.y = c * l1.y - sr * l0.y;
-        } else {
-          gsum = fma(l0.x, x0.y, gsum);
-          gsum = fma(-l0.y, x0.x, gsum);
-          gsum = fma(-l1.x, x1.y, gsum);
-          gsum = fma(l1.y, x1.x, gsum);
-          q0.x = c * x0.x - sr * x0.y; q0.y = c * x0.y + sr * x0.x;
-          q1.x = c * x1.x + sr * x1.y; q1.y = c * x1.y - sr * x1.x;
-          m0.x = c * l0.x - sr * l0.y; m0.y = c * l0.y + sr * l0.x;
-          m1.x = c * l1.x + sr * l1.y; m1.y = c * l1.y - sr * l1.x;
-        }
-        SP[p0] = q0;
-        SP[p1] = q1;
-        SL[p0] = m0;
-        SL[p1] = m1;
+        C x0 = SP[p0], x1 = SP[p1], l0 = SL[p0], l1 = SL[p1];
+        adj_pair<C, R>(op.gen, c, sr, x0, x1, l0, l1, gsum);
+        SP[p0] = x0;
+        SP[p1] = x1;
+        SL[p0] = l0;
+        SL[p1] = l1;
       }
+    } else {
+      // two rotations in one sweep: on the same bit each thread keeps its
+      // pairs, on two bits its quads, in registers between the two
+      const R c2 = csn[2 * op2->slot], s2 = csn[2 * op2->slot + 1];
+      R gsum2 = 0;
+      const int b1 = op.bit, b2 = op2->bit;
+      if (b1 == b2) {
+        for (int j = tid; j < (M >> 1); j += T) {
+          const int i0 = (int)insert_zero((uint64_t)j, b1);
+          const int i1 = i0 | (1 << b1);
+          const int p0 = PER == 2 ? aswz(i0) : i0;
+          const int p1 = PER == 2 ? aswz(i1) : i1;
+          C x0 = SP[p0], x1 = SP[p1], l0 = SL[p0], l1 = SL[p1];
+          adj_pair<C, R>(op.gen, c, sr, x0, x1, l0, l1, gsum);
+          adj_pair<C, R>(op2->gen, c2, s2, x0, x1, l0, l1, gsum2);
+          SP[p0] = x0;
+          SP[p1] = x1;
+          SL[p0] = l0;
+          SL[p1] = l1;
+        }
+      } else {
+        const int lo_b = b1 < b2 ? b1 : b2, hi_b = b1 < b2 ? b2 : b1;
+        for (int j = tid; j < (M >> 2); j += T) {
+          const int i00 =
+              (int)insert_zero(insert_zero((uint64_t)j, lo_b), hi_b);
+          const int i10 = i00 | (1 << b1), i01 = i00 | (1 << b2);
+          const int i11 = i10 | (1 << b2);
+          const int pa = PER == 2 ? aswz(i00) : i00;
+          const int pb = PER == 2 ? aswz(i10) : i10;
+          const int pc = PER == 2 ? aswz(i01) : i01;
+          const int pd = PER == 2 ? aswz(i11) : i11;
+          C xa = SP[pa], xb = SP[pb], xc = SP[pc], xd = SP[pd];
+          C la = SL[pa], lb = SL[pb], lc = SL[pc], ld = SL[pd];
+          // first rotation along b1: pairs (a, b), (c, d)
+          adj_pair<C, R>(op.gen, c, sr, xa, xb, la, lb, gsum);
+          adj_pair<C, R>(op.gen, c, sr, xc, xd, lc, ld, gsum);
+          // second along b2: pairs (a, c), (b, d)
+          adj_pair<C, R>(op2->gen, c2, s2, xa, xc, la, lc, gsum2);
+          adj_pair<C, R>(op2->gen, c2, s2, xb, xd, lb, ld, gsum2);
+          SP[pa] = xa;
+          SP[pb] = xb;
+          SP[pc] = xc;
+          SP[pd] = xd;
+          SL[pa] = la;
+          SL[pb] = lb;
+          SL[pc] = lc;
+          SL[pd] = ld;
+        }
+      }
+      adj_warp_partial<R>(gsum2, wred, op2->slot, T, tid);
+      ++oi;  // op2 is done
     }
     // warp partial now; the block reduction waits for the end of the stage
-    if constexpr (sizeof(R) == 4) {
-      float hi = gsum, lo = 0.f;
-      warp_sum_pair(hi, lo);
-      if ((tid & 31) == 0)
-        wred[op.slot * (T >> 5) + (tid >> 5)] = (double)hi + (double)lo;
-    } else {
-      const double gr = warp_sum_adj(gsum);
-      if ((tid & 31) == 0) wred[op.slot * (T >> 5) + (tid >> 5)] = gr;
-    }
+    adj_warp_partial<R>(gsum, wred, op.slot, T, tid);
     __syncthreads();  // the next op reads amplitudes this one wrote
   }
   // one block reduction for all rotations of the stage
