@@ -84,7 +84,10 @@ uint64_t gbsv_launch_count(void);
  * (src/unitair/simulation/operations.py:45-148) together with
  * apply_operator_tensor (:151-186) and act_first_qubits_tensor (:258-329):
  * the permute -> einsum -> permute sequence becomes one pass that addresses
- * amplitude pairs / quads by bit insertion.  qubits is a HOST array. */
+ * amplitude pairs / quads by bit insertion.  qubits is a HOST array.
+ * state_in == state_out (in place) is supported for k <= 5 (complex64) /
+ * k <= 4 (complex128) and k = 0; wider operators in place return
+ * GBSV_ERR_UNSUPPORTED. */
 int gbsv_apply_operator(const void* state_in, void* state_out, int dtype,
                         int num_qubits, int64_t num_states, int64_t in_stride,
                         const void* ops, int64_t op_stride,

@@ -92,3 +92,9 @@ def broadcast_strides(t: torch.Tensor, out_shape) -> list:
     strides = [0] * (nd - t.dim()) + list(t.stride())
     return [0 if s == 1 and o != 1 else st
             for s, st, o in zip(shape, strides, out_shape)]
+
+
+def max_inplace_qubits(dtype) -> int:
+    """Widest operator gbsv_apply_operator applies in place (state_in ==
+    state_out); wider ones go through a temporary."""
+    return 5 if dtype == torch.complex64 else 4

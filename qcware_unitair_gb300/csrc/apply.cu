@@ -353,7 +353,12 @@ static int apply_generic(const void* in, void* out, int dtype, int n,
     a.tmask |= uint64_t(1) << pos[j];
   }
   const int kmax_group = dtype == GBSV_C64 ? 5 : 4;
-  if (k >= 3 && k <= kmax_group && n >= k) {
+  const bool group = k >= 3 && k <= kmax_group && n >= k;
+  // the one-output-per-thread kernel reads other threads' inputs
+  if (!group && k >= 1 && in == out)
+    return set_error(GBSV_ERR_UNSUPPORTED,
+                     "a %d-qubit operator cannot be applied in place", k);
+  if (group) {
     uint64_t groups = a.total >> k;
     uint64_t gb = (groups + 127) / 128;
     const uint64_t gcap = (uint64_t)sm_count() * 32;

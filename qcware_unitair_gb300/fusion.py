@@ -730,10 +730,15 @@ class Program:
             else:
                 _, mat, qubits = op
                 op_stride = 0 if mat.dim() == 2 else mat.shape[-1] ** 2
+                wide = (cur.data_ptr() == out.data_ptr() and len(qubits) >
+                        _core.max_inplace_qubits(self.dtype))
+                dst = torch.empty_like(out) if wide else out
                 rc = L.gbsv_apply_operator(
-                    cur.data_ptr(), out.data_ptr(), self.code, self.n, B, N,
+                    cur.data_ptr(), dst.data_ptr(), self.code, self.n, B, N,
                     mat.data_ptr(), op_stride, _lib.qubit_array(qubits),
                     len(qubits), stream)
                 _lib.check(rc, "apply_operator")
+                if wide:
+                    out.copy_(dst)
             cur = out
         return out

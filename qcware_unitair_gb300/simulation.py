@@ -237,8 +237,15 @@ def apply_operator_(operator: torch.Tensor, qubits: Iterable[int],
         raise ValueError("apply_operator_ cannot broadcast an unbatched "
                          "state over an operator batch")
     if plan.num_states:
-        _launch_apply(plan.ops, plan.op_stride, state, 2 ** n, state, n,
-                      qubits, plan.num_states)
+        wide = k > _core.max_inplace_qubits(state.dtype)
+        if wide:  # the wide-operator kernel is not in place
+            out = torch.empty_like(state)
+            _launch_apply(plan.ops, plan.op_stride, state, 2 ** n, out, n,
+                          qubits, plan.num_states)
+            state.copy_(out)
+        else:
+            _launch_apply(plan.ops, plan.op_stride, state, 2 ** n, state, n,
+                          qubits, plan.num_states)
     return state
 
 

@@ -286,3 +286,20 @@ def test_stage_beyond_resident_limits(oracle, dtype, tol):
         out = prog.run(psi0.to(DEV))
         ref = oracle_run(oracle, circ, psi0.numpy())
         assert max_err(out.cpu().numpy(), ref) <= tol
+
+
+def test_program_with_wide_gate_in_place(oracle):
+    """A 6-qubit gate between stages of an in-place program."""
+    rng = np.random.default_rng(8)
+    n = 10
+    circ = Circuit(n)
+    for q in range(n):
+        circ.h(q)
+    circ.append(_haar(rng, 64), [0, 3, 4, 6, 8, 9], "dense")
+    for q in range(n):
+        circ.t(q)
+    psi0 = random_states(n, (2,), torch.complex64, seed=8)
+    st = psi0.to(DEV).clone()
+    circ.compile(torch.complex64, DEV).run(st, inplace=True)
+    ref = oracle_run(oracle, circ, psi0.numpy())
+    assert max_err(st.cpu().numpy(), ref) <= 1e-5

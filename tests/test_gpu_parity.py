@@ -307,13 +307,14 @@ def test_launch_counter_counts_kernels():
     assert _lib.launch_count() - before == 2
 
 
-@pytest.mark.parametrize("k", [3, 4, 5])
+@pytest.mark.parametrize("k", [3, 4, 5, 6])
 @pytest.mark.parametrize("dtype,tol", [(torch.complex64, 2e-6),
                                        (torch.complex128, 1e-13)])
 def test_wide_operators_group_kernel(oracle, k, dtype, tol):
-    """3- to 5-qubit operators (one thread per group of 2^k amplitudes):
-    shared and per-state matrices, target 0 among the targets or not, and
-    in place, against the complex128 oracle."""
+    """3- to 6-qubit operators (one thread per group of 2^k amplitudes, or
+    the wide-operator kernel through a temporary when in place): shared and
+    per-state matrices, target 0 among the targets or not, against the
+    complex128 oracle."""
     import qcware_unitair_gb300 as ug
     rng = np.random.default_rng(40 + k)
     n, B = 9, 3
