@@ -22,6 +22,7 @@ Multi-GPU: replicas only (each rank runs its own state), scaling "weak".
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -620,6 +621,8 @@ def run_gpu(args, ws, rank, local):
     torch.cuda.synchronize()
     events = []
     l0 = _lib.launch_count()
+    gc.collect()
+    gc.disable()  # no collector pauses inside the timed host loop
     with ClockSampler(local) as clocks:
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
@@ -629,6 +632,7 @@ def run_gpu(args, ws, rank, local):
         t1.record(stream)
         torch.cuda.synchronize()
     barrier()
+    gc.enable()
     launches = _lib.launch_count() - l0
     ms = t0.elapsed_time(t1)
     ms = max_over_ranks(ms, dev)
@@ -691,11 +695,14 @@ def run_gpu(args, ws, rank, local):
     torch.cuda.synchronize()
     barrier()
     e2e_steps = max(1, min(args.steps, 2))
+    gc.collect()
+    gc.disable()  # no collector pauses inside the timed host loop
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         e2e_step()
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0, dev)
+    gc.enable()
     e2e_value = bytes_per_gate * G * e2e_steps * ws / e2e_s / 1e9
     h2d = N * 8 + sum(m.numel() * 8 for m in mats_host)
     d2h = N * 8
