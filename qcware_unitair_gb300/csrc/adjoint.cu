@@ -342,10 +342,12 @@ __device__ __forceinline__ int aswz(int l) {
   return ((u ^ ((u >> 3) & 7)) << 1) | (l & 1);
 }
 
+// A fixed gate's adjoint (record g, values mp) on both tiles, psi and
+// lambda, in one sweep.
 template <typename R>
-__device__ __forceinline__ void adj_fixed(Cx<R>* S, int M, uint64_t base,
-                                          const FusedGate& g, const Cx<R>* mp,
-                                          Cx<R>& tscale) {
+__device__ __forceinline__ void adj_fixed(Cx<R>* SA, Cx<R>* SB, int M,
+                                          uint64_t base, const FusedGate& g,
+                                          const Cx<R>* mp) {
   using C = Cx<R>;
   constexpr int PER = 16 / sizeof(C);
   const int T = blockDim.x, tid = threadIdx.x;
@@ -355,9 +357,11 @@ __device__ __forceinline__ void adj_fixed(Cx<R>* S, int M, uint64_t base,
       const int i0 = (int)insert_zero((uint64_t)j, g.b0);
       const int i1 = i0 | (1 << g.b0);
       const int p0 = PER == 2 ? aswz(i0) : i0, p1 = PER == 2 ? aswz(i1) : i1;
-      const C x0 = S[p0], x1 = S[p1];
-      S[p0] = cmad(m1, x1, cmul(m0, x0));
-      S[p1] = cmad(m3, x1, cmul(m2, x0));
+      const C x0 = SA[p0], x1 = SA[p1], y0 = SB[p0], y1 = SB[p1];
+      SA[p0] = cmad(m1, x1, cmul(m0, x0));
+      SA[p1] = cmad(m3, x1, cmul(m2, x0));
+      SB[p0] = cmad(m1, y1, cmul(m0, y0));
+      SB[p1] = cmad(m3, y1, cmul(m2, y0));
     }
   } else if (g.kind == 1) {  // dense 4x4 on tile bits b0 (MSB), b1
     const int hi = g.b0 > g.b1 ? g.b0 : g.b1, lo = g.b0 > g.b1 ? g.b1 : g.b0;
@@ -365,22 +369,27 @@ __device__ __forceinline__ void adj_fixed(Cx<R>* S, int M, uint64_t base,
     for (int j = tid; j < (M >> 2); j += T) {
       const int i = (int)insert_zero(insert_zero((uint64_t)j, lo), hi);
       int p[4] = {i, i | M1, i | M0, i | M0 | M1};
-      C v[4];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
+      for (int k = 0; k < 4; ++k)
         if (PER == 2) p[k] = aswz(p[k]);
-        v[k] = S[p[k]];
-      }
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        C acc = cmul(mp[4 * r], v[0]);
-        acc = cmad(mp[4 * r + 1], v[1], acc);
-        acc = cmad(mp[4 * r + 2], v[2], acc);
-        acc = cmad(mp[4 * r + 3], v[3], acc);
-        S[p[r]] = acc;
+      for (int t = 0; t < 2; ++t) {
+        C* S = t ? SB : SA;
+        C v[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) v[k] = S[p[k]];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          C acc = cmul(mp[4 * r], v[0]);
+          acc = cmad(mp[4 * r + 1], v[1], acc);
+          acc = cmad(mp[4 * r + 2], v[2], acc);
+          acc = cmad(mp[4 * r + 3], v[3], acc);
+          S[p[r]] = acc;
+        }
       }
     }
-  } else {  // diagonal on nq qubits (tile bits or -1 - position)
+  } else {  // diagonal on nq qubits (tile bits or -1 - position); the
+            // caller handles gates with every qubit outside the tile
     int gidx = 0, lb0 = -1, lb1 = -1;
     for (int q = 0; q < g.nq; ++q) {
       const int b = q == 0 ? g.b0 : g.b1;
@@ -391,16 +400,15 @@ __device__ __forceinline__ void adj_fixed(Cx<R>* S, int M, uint64_t base,
       else
         lb1 = b;
     }
-    if (lb0 < 0 && lb1 < 0) {
-      if (threadIdx.x == 0) tscale = cmul(tscale, mp[gidx]);
-      return;
-    }
     for (int l = tid; l < M; l += T) {
       int idx = gidx;
       if (lb0 >= 0) idx |= ((l >> lb0) & 1) << (g.nq - 1);
       if (lb1 >= 0) idx |= ((l >> lb1) & 1);
+      const C f = mp[idx];
+      if (f.x == 1 && f.y == 0) continue;
       const int pl = PER == 2 ? aswz(l) : l;
-      S[pl] = cmul(mp[idx], S[pl]);
+      SA[pl] = cmul(f, SA[pl]);
+      SB[pl] = cmul(f, SB[pl]);
     }
   }
 }
@@ -542,8 +550,7 @@ __global__ void __launch_bounds__(512, sizeof(R) == 4 ? 2 : 1)
         }
         continue;
       }
-      adj_fixed<R>(SP, M, base, op.g, mp, scale_sh);
-      adj_fixed<R>(SL, M, base, op.g, mp, scale_sh);
+      adj_fixed<R>(SP, SL, M, base, op.g, mp);
       __syncthreads();
       continue;
     }
