@@ -61,6 +61,70 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// The same with V consecutive amplitudes (one 32-byte block) per thread:
+// for each term the partner amplitudes y = x ^ xmask of the block are again
+// one 32-byte block, read with one vector load, their order permuted by the
+// low bits of xmask.
+template <typename R, int V>
+__global__ void __launch_bounds__(256)
+    pauli_apply_block_kernel(const Cx<R>* psi, Cx<R>* out, uint64_t total,
+                             int n, const PauliTerm* terms, int num_terms) {
+  using C = Cx<R>;
+  __shared__ PauliTerm st[PAULI_MAX_TERMS];
+  for (int k = threadIdx.x; k < num_terms; k += blockDim.x) st[k] = terms[k];
+  __syncthreads();
+  const uint64_t nmask = (uint64_t(1) << n) - 1;
+  for (uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * V;
+       i < total; i += (uint64_t)gridDim.x * blockDim.x * V) {
+    const uint64_t x = i & nmask;  // block start, low log2(V) bits zero
+    const C* p = psi + (i - x);
+    R ar[V], ai[V];
+#pragma unroll
+    for (int e = 0; e < V; ++e) ar[e] = ai[e] = 0;
+    for (int k = 0; k < num_terms; ++k) {
+      const uint64_t xm = st[k].xmask, zm = st[k].zmask;
+      C b[V];
+      load_chunk<V>(p + ((x ^ xm) & ~uint64_t(V - 1)), b);
+      // b[e] holds amplitude ((x ^ xm) & ~(V-1)) + e; amplitude e of this
+      // thread's block needs partner (x + e) ^ xm, i.e. b[e ^ (xm & (V-1))]
+      if (xm & 1) {
+#pragma unroll
+        for (int e = 0; e < V; e += 2) {
+          const C t = b[e];
+          b[e] = b[e + 1];
+          b[e + 1] = t;
+        }
+      }
+      if constexpr (V == 4) {
+        if (xm & 2) {
+          C t = b[0];
+          b[0] = b[2];
+          b[2] = t;
+          t = b[1];
+          b[1] = b[3];
+          b[3] = t;
+        }
+      }
+      const R re = (R)st[k].re, im = (R)st[k].im;
+#pragma unroll
+      for (int e = 0; e < V; ++e) {
+        const uint64_t y = (x + e) ^ xm;
+        const R sgn = (__popcll(y & zm) & 1) ? R(-1) : R(1);
+        const R cr = sgn * re, ci = sgn * im;
+        ar[e] = fma(cr, b[e].x, fma(-ci, b[e].y, ar[e]));
+        ai[e] = fma(cr, b[e].y, fma(ci, b[e].x, ai[e]));
+      }
+    }
+    C o[V];
+#pragma unroll
+    for (int e = 0; e < V; ++e) {
+      o[e].x = ar[e];
+      o[e].y = ai[e];
+    }
+    store_chunk<V>(out + i, o);
+  }
+}
+
 struct AdjArgs {
   int n, pos;             // qubits, target bit position
   int gen;                // 0 = X, 1 = Y, 2 = Z
@@ -224,6 +288,27 @@ extern "C" int gbsv_pauli_sum_apply(const void* psi, void* out, int dtype,
   const uint64_t cap = (uint64_t)sm_count() * 16;
   if (blocks > cap) blocks = cap;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // 32-byte blocks need 4 (complex64) / 2 (complex128) amplitudes per state
+  // and 32-byte aligned buffers
+  const int V = dtype == GBSV_C64 ? 4 : 2;
+  if ((num_qubits >= 2 || (dtype != GBSV_C64 && num_qubits >= 1)) &&
+      (uintptr_t)psi % 32 == 0 && (uintptr_t)out % 32 == 0) {
+    uint64_t vb = (total / V + 255) / 256;
+    const uint64_t cap = (uint64_t)sm_count() * 32;
+    if (vb > cap) vb = cap;
+    if (vb < 1) vb = 1;
+    if (dtype == GBSV_C64)
+      pauli_apply_block_kernel<float, 4><<<(unsigned)vb, 256, 0, st>>>(
+          static_cast<const float2*>(psi), static_cast<float2*>(out), total,
+          num_qubits, static_cast<const PauliTerm*>(terms), num_terms);
+    else
+      pauli_apply_block_kernel<double, 2><<<(unsigned)vb, 256, 0, st>>>(
+          static_cast<const double2*>(psi), static_cast<double2*>(out),
+          total, num_qubits, static_cast<const PauliTerm*>(terms),
+          num_terms);
+    (void)V;
+    return after_launch("pauli_apply_block_kernel");
+  }
   if (dtype == GBSV_C64)
     pauli_apply_kernel<float><<<(unsigned)blocks, 256, 0, st>>>(
         static_cast<const float2*>(psi), static_cast<float2*>(out), total,

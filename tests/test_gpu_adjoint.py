@@ -173,3 +173,25 @@ def test_fused_backward_matches_unfused(n, layers, B, dtype):
     g2 = _backward_sweep(pc, params, H, psi_L, saved, dtype)
     tol = 1e-10 if dtype == torch.complex128 else 2e-5
     assert rel_err(g1.cpu(), g2.cpu()) < tol
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.complex64, 2e-6),
+                                       (torch.complex128, 1e-13)])
+@pytest.mark.parametrize("n", [1, 2, 3, 7])
+def test_pauli_apply_random_terms(dtype, tol, n):
+    """Random Pauli strings (X/Y/Z on any qubits, including the two lowest
+    index bits that permute amplitudes inside a 32-byte block)."""
+    rng = np.random.default_rng(10 + n)
+    H = PauliSum(n)
+    for _ in range(12):
+        k = int(rng.integers(1, n + 1))
+        qs = rng.choice(n, k, replace=False)
+        H.add(float(rng.normal()), {int(q): "XYZ"[int(rng.integers(3))]
+                                    for q in qs})
+    psi = random_states(n, (3,), dtype, seed=n)
+    lam = torch.empty_like(psi).to(DEV)
+    from qcware_unitair_gb300.adjoint import _pauli_apply
+    _pauli_apply(H, psi.to(DEV), lam)
+    ref = psi.numpy().astype(np.complex128) @ H.dense().T
+    assert np.abs(lam.cpu().numpy() - ref).max() <= tol * max(
+        1.0, np.abs(ref).max())
