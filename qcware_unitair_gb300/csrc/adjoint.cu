@@ -643,11 +643,21 @@ __global__ void __launch_bounds__(512, sizeof(R) == 4 ? 2 : 1)
     // a thread sums only its few pairs of the tile (plain FMA); precision
     // is kept where the sums grow: across lanes, warps and tiles
     R gsum = 0;
-    // the next op, when it is a rotation on a tile bit, shares this sweep
-    const AdjOp* op2 = nullptr;
-    if (op.bit >= 0 && oi + 1 < a.num_ops && a.ops[oi + 1].kind == 0 &&
-        a.ops[oi + 1].bit >= 0)
-      op2 = &a.ops[oi + 1];
+    // the following rotations on tile bits share this sweep while the run
+    // touches at most two bits (up to 4 rotations): pairs on one bit, quads
+    // on two, kept in registers between the rotations
+    int ng = 1, gb1 = op.bit, gb2 = -1;
+    if (op.bit >= 0) {
+      while (ng < 4 && oi + ng < a.num_ops) {
+        const AdjOp& nx = a.ops[oi + ng];
+        if (nx.kind != 0 || nx.bit < 0) break;
+        if (nx.bit != gb1 && nx.bit != gb2) {
+          if (gb2 >= 0) break;
+          gb2 = nx.bit;
+        }
+        ++ng;
+      }
+    }
     if (op.bit < 0) {
       // Z on a bit outside the tile: the tile sits at z = +/-1
       const int zb = (int)((base >> (-1 - op.bit)) & 1);
@@ -666,58 +676,59 @@ __global__ void __launch_bounds__(512, sizeof(R) == 4 ? 2 : 1)
         scale_sh = cmul(scale_sh, f);
         // a per-tile factor multiplies psi and lambda alike
       }
-    } else if (op2 == nullptr) {
-      const int b = op.bit;
-      for (int j = tid; j < (M >> 1); j += T) {
-        const int i0 = (int)insert_zero((uint64_t)j, b);
-        const int i1 = i0 | (1 << b);
-        const int p0 = PER == 2 ? aswz(i0) : i0, p1 = PER == 2 ? aswz(i1) : i1;
-        C x0 = SP[p0], x1 = SP[p1], l0 = SL[p0], l1 = SL[p1];
-        adj_pair<C, R>(op.gen, c, sr, x0, x1, l0, l1, gsum);
-        SP[p0] = x0;
-        SP[p1] = x1;
-        SL[p0] = l0;
-        SL[p1] = l1;
-      }
+      adj_warp_partial<R>(gsum, wred, op.slot, T, tid);
     } else {
-      // two rotations in one sweep: on the same bit each thread keeps its
-      // pairs, on two bits its quads, in registers between the two
-      const R c2 = csn[2 * op2->slot], s2 = csn[2 * op2->slot + 1];
-      R gsum2 = 0;
-      const int b1 = op.bit, b2 = op2->bit;
-      if (b1 == b2) {
+      R gs[4] = {0, 0, 0, 0};
+      R cc[4], ss[4];
+      int gen[4], bitk[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const AdjOp& rop = a.ops[oi + (r < ng ? r : 0)];
+        cc[r] = csn[2 * rop.slot];
+        ss[r] = csn[2 * rop.slot + 1];
+        gen[r] = rop.gen;
+        bitk[r] = rop.bit;
+      }
+      if (gb2 < 0) {
         for (int j = tid; j < (M >> 1); j += T) {
-          const int i0 = (int)insert_zero((uint64_t)j, b1);
-          const int i1 = i0 | (1 << b1);
+          const int i0 = (int)insert_zero((uint64_t)j, gb1);
+          const int i1 = i0 | (1 << gb1);
           const int p0 = PER == 2 ? aswz(i0) : i0;
           const int p1 = PER == 2 ? aswz(i1) : i1;
           C x0 = SP[p0], x1 = SP[p1], l0 = SL[p0], l1 = SL[p1];
-          adj_pair<C, R>(op.gen, c, sr, x0, x1, l0, l1, gsum);
-          adj_pair<C, R>(op2->gen, c2, s2, x0, x1, l0, l1, gsum2);
+#pragma unroll
+          for (int r = 0; r < 4; ++r)
+            if (r < ng)
+              adj_pair<C, R>(gen[r], cc[r], ss[r], x0, x1, l0, l1, gs[r]);
           SP[p0] = x0;
           SP[p1] = x1;
           SL[p0] = l0;
           SL[p1] = l1;
         }
       } else {
-        const int lo_b = b1 < b2 ? b1 : b2, hi_b = b1 < b2 ? b2 : b1;
+        const int lo_b = gb1 < gb2 ? gb1 : gb2, hi_b = gb1 < gb2 ? gb2 : gb1;
         for (int j = tid; j < (M >> 2); j += T) {
           const int i00 =
               (int)insert_zero(insert_zero((uint64_t)j, lo_b), hi_b);
-          const int i10 = i00 | (1 << b1), i01 = i00 | (1 << b2);
-          const int i11 = i10 | (1 << b2);
+          const int i10 = i00 | (1 << gb1), i01 = i00 | (1 << gb2);
+          const int i11 = i10 | (1 << gb2);
           const int pa = PER == 2 ? aswz(i00) : i00;
           const int pb = PER == 2 ? aswz(i10) : i10;
           const int pc = PER == 2 ? aswz(i01) : i01;
           const int pd = PER == 2 ? aswz(i11) : i11;
           C xa = SP[pa], xb = SP[pb], xc = SP[pc], xd = SP[pd];
           C la = SL[pa], lb = SL[pb], lc = SL[pc], ld = SL[pd];
-          // first rotation along b1: pairs (a, b), (c, d)
-          adj_pair<C, R>(op.gen, c, sr, xa, xb, la, lb, gsum);
-          adj_pair<C, R>(op.gen, c, sr, xc, xd, lc, ld, gsum);
-          // second along b2: pairs (a, c), (b, d)
-          adj_pair<C, R>(op2->gen, c2, s2, xa, xc, la, lc, gsum2);
-          adj_pair<C, R>(op2->gen, c2, s2, xb, xd, lb, ld, gsum2);
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            if (r >= ng) continue;
+            if (bitk[r] == gb1) {  // pairs (a, b), (c, d)
+              adj_pair<C, R>(gen[r], cc[r], ss[r], xa, xb, la, lb, gs[r]);
+              adj_pair<C, R>(gen[r], cc[r], ss[r], xc, xd, lc, ld, gs[r]);
+            } else {  // along gb2: pairs (a, c), (b, d)
+              adj_pair<C, R>(gen[r], cc[r], ss[r], xa, xc, la, lc, gs[r]);
+              adj_pair<C, R>(gen[r], cc[r], ss[r], xb, xd, lb, ld, gs[r]);
+            }
+          }
           SP[pa] = xa;
           SP[pb] = xb;
           SP[pc] = xc;
@@ -728,11 +739,12 @@ __global__ void __launch_bounds__(512, sizeof(R) == 4 ? 2 : 1)
           SL[pd] = ld;
         }
       }
-      adj_warp_partial<R>(gsum2, wred, op2->slot, T, tid);
-      ++oi;  // op2 is done
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+        if (r < ng)
+          adj_warp_partial<R>(gs[r], wred, a.ops[oi + r].slot, T, tid);
+      oi += ng - 1;  // the group's other rotations are done
     }
-    // warp partial now; the block reduction waits for the end of the stage
-    adj_warp_partial<R>(gsum, wred, op.slot, T, tid);
     __syncthreads();  // the next op reads amplitudes this one wrote
   }
   // one block reduction for all rotations of the stage
