@@ -1,7 +1,7 @@
 /*
  * CPU oracle for the state-vector hot path.  TEST INFRASTRUCTURE ONLY:
- * imported by tests/, by __graft_entry__.smoke() as the checker, and by
- * bench.py's CPU-baseline / reference arm.  The engine never calls it.
+ * imported by tests/, by __graft_entry__.smoke() to check its result, and
+ * by bench.py's CPU-baseline / reference arm.  The engine never calls it.
  *
  * It restates, in plain C, what unitair computes for
  *   apply_operator   src/unitair/simulation/operations.py:45-148

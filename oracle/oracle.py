@@ -1,6 +1,6 @@
 """CPU oracle for the unitair hot path -- TEST INFRASTRUCTURE ONLY.
 
-Only ``tests/``, ``__graft_entry__.smoke()`` (as the checker) and
+Only ``tests/``, ``__graft_entry__.smoke()`` (to check its result) and
 ``bench.py`` (CPU baseline / reference arm) may import this module.  The
 engine in ``qcware_unitair_gb300`` never does.
 
