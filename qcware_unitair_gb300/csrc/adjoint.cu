@@ -539,7 +539,10 @@ __device__ __forceinline__ void adj_pair(int gen, R c, R sr, C& x0, C& x1,
   l1 = m1;
 }
 
-// Warp partial of a rotation's gradient into wred[slot * warps + warp].
+// Warp partial of a rotation's gradient into wred[slot * warps + warp]:
+// for complex64 the float pair itself (8 bytes), converted to double only
+// in the end-of-stage reduction, where the lanes run over rotation slots
+// (a conversion here would be a whole FP64 warp instruction per rotation).
 template <typename R>
 __device__ __forceinline__ void adj_warp_partial(R gsum, double* wred,
                                                  int slot, int T, int tid) {
@@ -547,7 +550,8 @@ __device__ __forceinline__ void adj_warp_partial(R gsum, double* wred,
     float hi = gsum, lo = 0.f;
     warp_sum_pair(hi, lo);
     if ((tid & 31) == 0)
-      wred[slot * (T >> 5) + (tid >> 5)] = (double)hi + (double)lo;
+      reinterpret_cast<float2*>(wred)[slot * (T >> 5) + (tid >> 5)] =
+          make_float2(hi, lo);
   } else {
     const double gr = warp_sum_adj(gsum);
     if ((tid & 31) == 0) wred[slot * (T >> 5) + (tid >> 5)] = gr;
@@ -752,7 +756,14 @@ __global__ void __launch_bounds__(512, sizeof(R) == 4 ? 2 : 1)
     const int warps = T >> 5;
     for (int k = tid; k < a.num_slots; k += T) {
       double t = 0.0;
-      for (int w = 0; w < warps; ++w) t += wred[k * warps + w];
+      for (int w = 0; w < warps; ++w) {
+        if constexpr (sizeof(R) == 4) {
+          const float2 q = reinterpret_cast<const float2*>(wred)[k * warps + w];
+          t += (double)q.x + (double)q.y;
+        } else {
+          t += wred[k * warps + w];
+        }
+      }
       partial[(uint64_t)k * gridDim.x + blockIdx.x] = t;
     }
   }
