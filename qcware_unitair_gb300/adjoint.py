@@ -509,6 +509,98 @@ def _plan_backward(pc: ParamCircuit, a: int, b: int, dtype, dev, m: int):
     return out
 
 
+def _plan_backward_native(pc: ParamCircuit, a: int, b: int, dtype, dev,
+                          m: int):
+    """_plan_backward with the stages planned by gbsv_plan (C++) and the
+    adjoint records assembled by column: the same stages, records and
+    values (one pool for all stages instead of one per stage)."""
+    from .fusion import (DESC_DTYPE, _KIND_CODE, _to_device, native_plan)
+    n = pc.num_qubits
+    ops = list(reversed(pc.ops[a:b]))
+    G = len(ops)
+    desc = np.zeros(max(1, G), dtype=DESC_DTYPE)
+    parts = [np.eye(2, dtype=np.complex128).reshape(-1)]  # rotations' stand-in
+    off = 4
+    kinds, nqs, q0s, q1s, offs = [], [], [], [], []
+    is_rot = np.zeros(G, dtype=bool)
+    gens = np.zeros(G, np.int32)
+    pidxs = np.zeros(G, np.int32)
+    scales = np.zeros(G, np.float64)
+    dag = {}  # adjoints of repeated fixed matrices (the same object)
+    for i, op in enumerate(ops):
+        if op[0] == "rot":
+            _, gen, q, pi, scale = op
+            kinds.append(_KIND_CODE[DIAG if gen == "Z" else DENSE])
+            nqs.append(1)
+            q0s.append(q)
+            q1s.append(0)
+            offs.append(0)
+            is_rot[i] = True
+            gens[i], pidxs[i], scales[i] = GEN[gen], pi, scale
+        else:
+            _, mat, qs, kind = op
+            md = dag.get(id(mat))
+            if md is None:
+                md = np.ascontiguousarray(
+                    np.conj(mat.detach().cpu().numpy()).T,
+                    dtype=np.complex128).reshape(-1)
+                dag[id(mat)] = md
+            kinds.append(_KIND_CODE[kind or DENSE])
+            nqs.append(len(qs))
+            q0s.append(qs[0])
+            q1s.append(qs[1] if len(qs) > 1 else 0)
+            offs.append(off)
+            parts.append(md)
+            off += md.size
+    if G:
+        desc["kind"][:G], desc["nq"][:G] = kinds, nqs
+        desc["q0"][:G], desc["q1"][:G], desc["mat"][:G] = q0s, q1s, offs
+        desc["num_batch"][:G] = 1
+    mats = np.ascontiguousarray(np.concatenate(parts))
+    c_min = min(4 if dtype == torch.complex64 else 3, m)
+    nat = native_plan(None, n, m, c_min, 0, True, dtype, desc[:G], mats)
+    recs = nat["records"]
+    pool = torch.from_numpy(nat["pool"]).to(dev) if len(nat["pool"]) else \
+        torch.zeros(1, dtype=dtype, device=dev)
+    AD = _adjop_dtype()
+    out = []
+    nxt = 0  # next gate index not yet placed
+    for op in nat["ops"]:
+        t, first, count = int(op["type"]), int(op["first"]), int(op["count"])
+        if t == 0:
+            assert first == nxt
+            src = ops[first]
+            out.append(("rot" if src[0] == "rot" else "fixed", src))
+            nxt = first + 1
+            continue
+        idx = np.arange(nxt, nxt + count)
+        nxt += count
+        r = recs[first:first + count]
+        rot = is_rot[idx]
+        ad = np.zeros(count, dtype=AD)
+        ad["kind"] = np.where(rot, 0, 1)
+        ad["gen"] = gens[idx]
+        ad["bit"] = np.where(rot, r["b0"], 0)
+        ad["slot"] = np.where(rot, np.cumsum(rot) - 1, 0)
+        ad["pidx"] = np.where(rot, pidxs[idx], 0)
+        ad["scale"] = np.where(rot, scales[idx], 0.0)
+        ad["g"][~rot] = r[~rot]
+        out.append(("stage", {
+            "c": int(op["contiguous"]),
+            "positions": (ctypes_int32 * m)(
+                *[int(x) for x in op["positions"][:m]]),
+            "ops": _to_device(ad.view(np.uint8), dev),
+            "num_ops": count,
+            "pool": pool,
+            "num_slots": int(rot.sum()),
+            "slot_param": torch.tensor(pidxs[idx][rot].tolist() or [0],
+                                       dtype=torch.int32, device=dev),
+            "slot_scale": torch.tensor(scales[idx][rot].tolist() or [0.0],
+                                       dtype=torch.float64, device=dev)}))
+    assert nxt == G
+    return out
+
+
 def _backward_fused(pc, params, H, psi_L, saved, dtype):
     """The adjoint sweep with fused backward stages (see the kernel
     gbsv_adjoint_stage): one read and write of psi and lambda per stage."""
@@ -537,7 +629,10 @@ def _backward_fused(pc, params, H, psi_L, saved, dtype):
         a, b = segs[si]
         key = (a, b, dtype, str(dev), m)
         if key not in cache:
-            cache[key] = _plan_backward(pc, a, b, dtype, dev, m)
+            host = all(op[0] == "rot" or not op[1].is_cuda
+                       for op in pc.ops[a:b])
+            cache[key] = (_plan_backward_native if host else _plan_backward)(
+                pc, a, b, dtype, dev, m)
         for entry in cache[key]:
             if entry[0] == "stage":
                 st = entry[1]

@@ -36,7 +36,7 @@ import numpy as np
 import torch
 
 from . import _core, _lib, simulation, states
-from .circuits import Gate, random_circuit, ROTATIONS
+from .circuits import Gate, gate_matrix, random_circuit, ROTATIONS
 from .fusion import (FG_DTYPE, Program, gate_list_desc, native_plan)
 
 
@@ -126,6 +126,22 @@ def _outputs(psi: torch.Tensor, n: int):
     return halves.sum(-1), halves[:, 0] - halves[:, 1]
 
 
+_FIXED_GATES: Dict[str, tuple] = {}
+
+
+def _fixed_gate(name: str):
+    """One matrix tensor per canonical fixed gate (planners reuse the same
+    object's adjoint) and its structure: CZ / Z / S / T diagonal, CNOT
+    controlled, the rest dense."""
+    ent = _FIXED_GATES.get(name)
+    if ent is None:
+        from .fusion import _NAMED_KIND, DENSE
+        ent = _FIXED_GATES[name] = (
+            torch.as_tensor(gate_matrix(name).astype(np.complex128)),
+            _NAMED_KIND.get(name, DENSE))
+    return ent
+
+
 def _grad_circuit(req: Request):
     """ParamCircuit with one parameter per rotation (angles shared by the
     request's states) and <Z_0> as the observable."""
@@ -139,7 +155,9 @@ def _grad_circuit(req: Request):
                 g.qubits[0], len(angles))
             angles.append(g.theta)
         else:
-            pc.gate(g.matrix(), g.qubits)
+            mat, kind = _fixed_gate(g.name)
+            pc.ops.append(("fixed", mat, tuple(int(q) for q in g.qubits),
+                           kind))
     return pc, PauliSum(req.num_qubits).z(0), angles
 
 

@@ -45,3 +45,53 @@ def test_param_validation():
         pc.ry(2, 0)
     with pytest.raises(ValueError):
         PauliSum(2).add(1.0, {0: "Q"})
+
+
+def _cmp_backward_plans(pc, m, dtype):
+    """The backward-stage plan built by the C++ planner equals the one the
+    Python planner builds: same stage order, bit positions, adjoint
+    operation records, fixed-gate records, matrices and parameter slots."""
+    import torch
+    from qcware_unitair_gb300.adjoint import (_adjop_dtype, _plan_backward,
+                                              _plan_backward_native)
+    cpu = torch.device("cpu")
+    A = _plan_backward(pc, 0, len(pc.ops), dtype, cpu, m)
+    B = _plan_backward_native(pc, 0, len(pc.ops), dtype, cpu, m)
+    assert len(A) == len(B)
+    AD = _adjop_dtype()
+    for (ka, ea), (kb, eb) in zip(A, B):
+        assert ka == kb
+        if ka != "stage":
+            assert ea is eb or ea == eb
+            continue
+        assert ea["c"] == eb["c"]
+        assert list(ea["positions"]) == list(eb["positions"])
+        xa, xb = ea["ops"].numpy().view(AD), eb["ops"].numpy().view(AD)
+        for f in ("kind", "gen", "bit", "slot", "pidx", "scale"):
+            assert np.array_equal(xa[f], xb[f]), f
+        fixed = xa["kind"] == 1
+        ga, gb = xa["g"][fixed], xb["g"][fixed]
+        for f in ("kind", "nq", "b0", "b1", "cmask", "cval", "mat_bstride"):
+            assert np.array_equal(ga[f], gb[f]), f
+        pa, pb = ea["pool"].numpy(), eb["pool"].numpy()
+        for ia, ib in zip(ga, gb):
+            k = (16 if ia["kind"] == 1 else
+                 (1 << ia["nq"] if ia["kind"] == 2 else 4))
+            assert np.array_equal(pa[ia["mat"]:ia["mat"] + k],
+                                  pb[ib["mat"]:ib["mat"] + k])
+        assert torch.equal(ea["slot_param"], eb["slot_param"])
+        assert torch.equal(ea["slot_scale"], eb["slot_scale"])
+
+
+@pytest.mark.parametrize("dtype", ["complex64", "complex128"])
+def test_native_backward_plan_matches_python(dtype):
+    import torch
+    from qcware_unitair_gb300 import serve as S
+    dt = getattr(torch, dtype)
+    for n, layers in ((8, 3), (20, 4)):
+        _cmp_backward_plans(hardware_efficient_ansatz(n, layers),
+                            min(12, n), dt)
+    for req in S.make_trace(6, rate=100.0, seed=0, qubits=(10, 20),
+                            depth=(50, 300)):
+        pc, _, _ = S._grad_circuit(req)
+        _cmp_backward_plans(pc, min(12, req.num_qubits), dt)
