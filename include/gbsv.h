@@ -222,7 +222,8 @@ size_t gbsv_sample_scratch_bytes(int64_t dim);
 
 /* Draw num_samples basis indices from |state|^2 / sum |state|^2 (one state
  * of dim = 2^n amplitudes) into out_indices (device int64).  Samples are a
- * pure function of (seed, sample number).  Replaces the sampling in
+ * pure function of (seed, sample number).  state and scratch 16-byte
+ * aligned.  Replaces the sampling in
  * unitair's measure (src/unitair/simulation/measurement.py:9-70). */
 int gbsv_sample(const void* state, int dtype, int64_t dim,
                 int64_t num_samples, uint64_t seed, int64_t* out_indices,

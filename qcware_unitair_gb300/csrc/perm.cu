@@ -159,10 +159,11 @@ __global__ void __launch_bounds__(256)
 
 // ---- sampling ----------------------------------------------------------
 // Three tables over the state: SUB[i] = sum |psi|^2 over 32-amplitude group
-// i, SUMS[c] over 1024-amplitude chunk c (32 groups), CDF = inclusive
-// prefix of SUMS.  A sample binary-searches CDF for its chunk, then one warp
-// scans the chunk's 32 group sums and the chosen group's 32 amplitudes:
-// 32 + 32 reads instead of up to 1024.
+// i (FP32), SUMS[c] over 1024-amplitude chunk c (32 groups, FP64), CDF =
+// inclusive prefix of SUMS.  A sample binary-searches CDF for its chunk,
+// then scans the chunk's 32 group sums and the chosen group's 32
+// amplitudes: 32 + 32 reads instead of up to 1024.  One thread per sample,
+// so a warp has 32 independent searches in flight.
 constexpr int CHUNK = 1024;
 constexpr int GROUP = 32;
 
@@ -170,7 +171,7 @@ constexpr int GROUP = 32;
 template <typename R>
 __global__ void __launch_bounds__(256)
     chunk_sum_kernel(const Cx<R>* psi, uint64_t num_chunks, uint64_t dim,
-                     double* sums, double* subs) {
+                     double* sums, float* subs) {
   const int lane = threadIdx.x & 31;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   for (uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -209,10 +210,59 @@ __global__ void __launch_bounds__(256)
       }
     }
     double g = acc.value();
-    subs[c * GROUP + lane] = g;
+    subs[c * GROUP + lane] = (float)g;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
     if (lane == 0) sums[c] = g;
+  }
+}
+
+// complex64 states of whole chunks: one warp per chunk with coalesced
+// loads.  Load j reads float4 j * 32 + lane (amplitudes 64 j + 2 lane and
+// + 1), so lanes 0-15 cover group 2 j and lanes 16-31 group 2 j + 1.  A
+// butterfly over the 16 lanes of each half (keep one half of the values,
+// send the other) leaves lane l with the sum of group 2 (l & 15) + (l >> 4).
+// The chunk sum adds the 32 rounded group sums with an error-free FP32
+// two-sum, so the chunk CDF and the group sums agree.
+__global__ void __launch_bounds__(256)
+    chunk_sum_c64_kernel(const float4* psi, uint64_t num_chunks,
+                         double* sums, float* subs) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+       c < num_chunks; c += nwarps) {
+    const float4* src = psi + c * (CHUNK / 2);
+    float4 q[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) q[j] = src[j * 32 + lane];
+    float p[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j)
+      p[j] = fmaf(q[j].x, q[j].x,
+                  fmaf(q[j].y, q[j].y, fmaf(q[j].z, q[j].z, q[j].w * q[j].w)));
+#pragma unroll
+    for (int k = 8; k > 0; k >>= 1) {
+      const bool up = (lane & k) != 0;
+#pragma unroll
+      for (int i = 0; i < k; ++i) {
+        const float send = up ? p[i] : p[i + k];
+        const float keep = up ? p[i + k] : p[i];
+        p[i] = keep + __shfl_xor_sync(0xffffffffu, send, k);
+      }
+    }
+    const float g = p[0];
+    subs[c * GROUP + 2 * (lane & 15) + (lane >> 4)] = g;
+    float hi = g, lo = 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+      const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+      const float t = hi + oh;
+      const float bp = t - hi;
+      lo += ol + ((hi - (t - bp)) + (oh - bp));
+      hi = t;
+    }
+    if (lane == 0) sums[c] = (double)hi + (double)lo;
   }
 }
 
@@ -300,14 +350,40 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
   return z ^ (z >> 31);
 }
 
+// Picks, from a run of non-negative values v[0..k), the first k with
+// v[k] > 0 and (inclusive prefix) > rem; without one, the last v[k] > 0
+// (rounding can leave rem just above the run's own sum).  *excl_out = the
+// exclusive prefix of the pick.
+struct Pick {
+  float excl = 0.f, pick_excl = 0.f, last_excl = 0.f;
+  int pick = -1, last = -1;
+  __device__ __forceinline__ void add(float v, int k, float rem) {
+    const float incl = excl + v;
+    if (v > 0.f) {
+      if (pick < 0 && incl > rem) {
+        pick = k;
+        pick_excl = excl;
+      }
+      last = k;
+      last_excl = excl;
+    }
+    excl = incl;
+  }
+  __device__ __forceinline__ int result(float* excl_out) const {
+    if (pick >= 0) {
+      *excl_out = pick_excl;
+      return pick;
+    }
+    *excl_out = last_excl;
+    return last;
+  }
+};
+
 template <typename R>
 __global__ void __launch_bounds__(256)
-    sample_kernel(const Cx<R>* psi, const double* cdf, const double* subs,
+    sample_kernel(const Cx<R>* psi, const double* cdf, const float* subs,
                   uint64_t num_chunks, uint64_t dim, uint64_t num_samples,
                   uint64_t seed, int64_t* out) {
-  const int lane = threadIdx.x & 31;
-  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   const double total = cdf[num_chunks - 1];
   // every stride-th CDF value in shared memory: the first levels of the
   // search stay on chip
@@ -321,7 +397,9 @@ __global__ void __launch_bounds__(256)
     coarse[i] = cdf[e - 1];
   }
   __syncthreads();
-  for (uint64_t sidx = warp; sidx < num_samples; sidx += nwarps) {
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t sidx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+       sidx < num_samples; sidx += nthreads) {
     const uint64_t h = mix64(seed ^ mix64(sidx));
     const double u = (double)(h >> 11) * (1.0 / 9007199254740992.0) * total;
     // first chunk whose inclusive prefix exceeds u: coarse block, then
@@ -340,40 +418,57 @@ __global__ void __launch_bounds__(256)
       if (cdf[mid] > u) hi = mid; else lo = mid + 1;
     }
     const double run = lo ? cdf[lo - 1] : 0.0;
-    const uint64_t base = lo * CHUNK;
     // the rest of u inside the chunk; FP32 from here (a chunk's share only)
     float rem = (float)(u - run);
-    // the chunk's 32 group sums, then the chosen group's 32 amplitudes
-    const float gs = (float)subs[lo * GROUP + lane];
-    float gi = gs;
+    // the chunk's 32 group sums: 128 contiguous bytes
+    Pick gp;
+    {
+      const float4* sv = reinterpret_cast<const float4*>(subs + lo * GROUP);
+      float4 q[GROUP / 4];
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const float t = __shfl_up_sync(0xffffffffu, gi, o);
-      if (lane >= o) gi += t;
-    }
-    unsigned hit = __ballot_sync(0xffffffffu, gs > 0.f && gi > rem);
-    const unsigned gnz = __ballot_sync(0xffffffffu, gs > 0.f);
-    // rounding can leave u just above the chunk's own running sum
-    const int grp = hit ? __ffs(hit) - 1 : (gnz ? 31 - __clz(gnz) : 0);
-    rem -= __shfl_sync(0xffffffffu, gi - gs, grp);
-    const uint64_t gbase = base + (uint64_t)grp * GROUP;
-    float p = 0.f;
-    if (gbase + lane < dim) {
-      const Cx<R> v = psi[gbase + lane];
-      p = (float)((R)v.x * v.x + (R)v.y * v.y);
-    }
-    float incl = p;
+      for (int k = 0; k < GROUP / 4; ++k) q[k] = sv[k];
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const float t = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += t;
+      for (int k = 0; k < GROUP / 4; ++k) {
+        gp.add(q[k].x, 4 * k, rem);
+        gp.add(q[k].y, 4 * k + 1, rem);
+        gp.add(q[k].z, 4 * k + 2, rem);
+        gp.add(q[k].w, 4 * k + 3, rem);
+      }
     }
-    hit = __ballot_sync(0xffffffffu, p > 0.f && incl > rem);
-    const unsigned nz = __ballot_sync(0xffffffffu, p > 0.f);
-    const int64_t found =
-        hit ? (int64_t)gbase + __ffs(hit) - 1
-            : (nz ? (int64_t)gbase + 31 - __clz(nz) : (int64_t)gbase);
-    if (lane == 0) out[sidx] = found;
+    float gex;
+    int grp = gp.result(&gex);
+    if (grp < 0) grp = 0;
+    rem -= gex;
+    const uint64_t gbase = lo * CHUNK + (uint64_t)grp * GROUP;
+    Pick ap;
+    if (gbase + GROUP <= dim) {
+      // the group's amplitudes in 128-byte batches of 16-byte loads
+      constexpr int PER = 16 / (int)sizeof(Cx<R>);  // amplitudes per load
+      constexpr int BATCH = 8;                       // loads per batch
+      const uint4* av = reinterpret_cast<const uint4*>(psi + gbase);
+#pragma unroll
+      for (int b = 0; b < GROUP / (PER * BATCH); ++b) {
+        uint4 q[BATCH];
+#pragma unroll
+        for (int k = 0; k < BATCH; ++k) q[k] = av[b * BATCH + k];
+#pragma unroll
+        for (int k = 0; k < BATCH; ++k) {
+          const Cx<R>* c = reinterpret_cast<const Cx<R>*>(&q[k]);
+#pragma unroll
+          for (int e = 0; e < PER; ++e)
+            ap.add((float)((R)c[e].x * c[e].x + (R)c[e].y * c[e].y),
+                   (b * BATCH + k) * PER + e, rem);
+        }
+      }
+    } else {
+      for (int k = 0; gbase + k < dim && k < GROUP; ++k) {
+        const Cx<R> c = psi[gbase + k];
+        ap.add((float)((R)c.x * c.x + (R)c.y * c.y), k, rem);
+      }
+    }
+    float aex;
+    const int a = ap.result(&aex);
+    out[sidx] = (int64_t)gbase + (a < 0 ? 0 : a);
   }
 }
 
@@ -542,7 +637,9 @@ static uint64_t sample_chunks(int64_t dim) {
 extern "C" size_t gbsv_sample_scratch_bytes(int64_t dim) {
   if (dim <= 0) return 0;
   const uint64_t chunks = sample_chunks(dim);
-  return (size_t)(chunks * (2 + GROUP) + 1024) * sizeof(double);
+  // sums and CDF (FP64), group sums (FP32), scan totals
+  return (size_t)(chunks * 2 + 1024) * sizeof(double) +
+         (size_t)chunks * GROUP * sizeof(float);
 }
 
 extern "C" int gbsv_sample(const void* state, int dtype, int64_t dim,
@@ -564,18 +661,24 @@ extern "C" int gbsv_sample(const void* state, int dtype, int64_t dim,
   if (!scratch || scratch_bytes < need)
     return set_error(GBSV_ERR_SCRATCH, "sampling needs %zu scratch bytes",
                      need);
+  if ((uintptr_t)state % 16 || (uintptr_t)scratch % 16)
+    return set_error(GBSV_ERR_INVALID_ARG,
+                     "state and scratch must be 16-byte aligned");
   if (chunks > 0x7fffffffull)
     return set_error(GBSV_ERR_UNSUPPORTED, "state too large");
   double* sums = static_cast<double*>(scratch);
   double* cdf = sums + chunks;
-  double* subs = cdf + chunks;
-  double* tot = subs + chunks * GROUP;
+  double* tot = cdf + chunks;
+  float* subs = reinterpret_cast<float*>(tot + 1024);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   {
     uint64_t blocks = (chunks * 32 + 255) / 256;
     const uint64_t cap = (uint64_t)sm_count() * 16;
     if (blocks > cap) blocks = cap;
-    if (dtype == GBSV_C64)
+    if (dtype == GBSV_C64 && dim % CHUNK == 0)
+      chunk_sum_c64_kernel<<<(unsigned)blocks, 256, 0, st>>>(
+          static_cast<const float4*>(state), chunks, sums, subs);
+    else if (dtype == GBSV_C64)
       chunk_sum_kernel<float><<<(unsigned)blocks, 256, 0, st>>>(
           static_cast<const float2*>(state), chunks, (uint64_t)dim, sums, subs);
     else
@@ -598,9 +701,8 @@ extern "C" int gbsv_sample(const void* state, int dtype, int64_t dim,
   scan_blocks_kernel<<<nseg, 1024, 0, st>>>(sums, chunks, seg, tot, cdf);
   rc = after_launch("scan_blocks_kernel");
   if (rc) return rc;
-  const uint64_t warps = (uint64_t)num_samples;
-  uint64_t blocks = (warps * 32 + 255) / 256;
-  const uint64_t cap = (uint64_t)sm_count() * 16;
+  uint64_t blocks = ((uint64_t)num_samples + 255) / 256;
+  const uint64_t cap = (uint64_t)sm_count() * 8;
   if (blocks > cap) blocks = cap;
   if (dtype == GBSV_C64)
     sample_kernel<float><<<(unsigned)blocks, 256, 0, st>>>(

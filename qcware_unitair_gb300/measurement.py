@@ -25,6 +25,8 @@ def sample(state: torch.Tensor, num_samples: int,
     if seed is None:
         seed = int(torch.randint(0, 2 ** 62, (1,)).item())
     s = state.contiguous()
+    if s.data_ptr() % 16:  # a view at an odd offset: vector loads need 16
+        s = s.clone()
     out = torch.empty(int(num_samples), dtype=torch.int64, device=s.device)
     L = _lib.load()
     nbytes = int(L.gbsv_sample_scratch_bytes(s.numel()))

@@ -150,3 +150,19 @@ def test_random_permutations_tiled(n, dtype):
             [0] + [1 + p for p in perm]).reshape(B, -1)
         got = ug.permute_qubits(perm, st).cpu().numpy()
         assert np.array_equal(got, ref)
+
+
+def test_measure_offset_view():
+    """A state viewed at an 8-byte offset (not 16-byte aligned) samples
+    like the same state copied to an aligned buffer."""
+    n = 12
+    rng = np.random.default_rng(4)
+    amps = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+    amps /= np.linalg.norm(amps)
+    big = torch.zeros(2 ** n + 1, dtype=torch.complex64, device=DEV)
+    big[1:] = cu(amps.astype(np.complex64))
+    view = big[1:]
+    assert view.data_ptr() % 16 == 8
+    a = ug.measurement.sample(view, 5000, seed=2).cpu().numpy()
+    b = ug.measurement.sample(view.clone(), 5000, seed=2).cpu().numpy()
+    assert np.array_equal(a, b)
