@@ -180,7 +180,8 @@ int gbsv_run_stage_layouts(const void* state_in, void* state_out, int dtype,
 /* Many circuits in one launch: CTA i runs gates[gate_first[i] ..
  * gate_first[i] + gate_count[i]) (records as for gbsv_run_stage with the
  * whole state as the tile, i.e. tile bit b = amplitude-index bit b) on the
- * state of 2^num_qubits amplitudes at state_ptrs[i], in place.  state_ptrs
+ * state of 2^num_qubits amplitudes at state_ptrs[i], in place (each state
+ * 16-byte aligned; a CTA whose state is not leaves it untouched).  state_ptrs
  * (uint64), gate_first and gate_count (int32) are device arrays of num_ctas
  * entries.  num_qubits <= gbsv_fused_max_tile_qubits(dtype).  This is the
  * batched launch of the serving loop: requests with different circuits and
@@ -362,7 +363,8 @@ typedef struct gbsv_adjoint_op {
  * tiles in index order) to grad[s * num_params + slot_param[k]].
  * slot_param / slot_scale are device arrays of num_slots entries; scratch
  * holds num_slots * num_states * (2^(n - tile_qubits) + 2) doubles (tile
- * partials, then the cos / sin of every rotation per state). */
+ * partials, then the cos / sin of every rotation per state).  psi and lam
+ * 16-byte aligned. */
 int gbsv_adjoint_stage(void* psi, void* lam, int dtype, int num_qubits,
                        int64_t num_states, int tile_qubits,
                        int contiguous_qubits, const int32_t* tile_positions,

@@ -844,6 +844,9 @@ extern "C" int gbsv_adjoint_stage(
       (num_ops > 0 && (!ops || !pool)) ||
       (num_slots > 0 && (!params || !slot_param || !slot_scale || !grad)))
     return set_error(GBSV_ERR_INVALID_ARG, "null or aliased pointer");
+  if ((uintptr_t)psi % 16 || (uintptr_t)lam % 16)
+    return set_error(GBSV_ERR_INVALID_ARG,
+                     "psi and lambda must be 16-byte aligned");
   AdjStageArgs a{};
   a.n = n;
   a.m = m;

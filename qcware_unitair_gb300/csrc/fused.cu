@@ -1435,6 +1435,9 @@ __global__ void __launch_bounds__(512, 2)
   const int T = blockDim.x;
   const int tid = threadIdx.x;
   C* st = reinterpret_cast<C*>(states[blockIdx.x]);
+  // 16-byte copies: a misaligned state is left untouched (the whole CTA
+  // returns before its first barrier)
+  if (reinterpret_cast<uintptr_t>(st) % 16) return;
   constexpr int PER = 16 / sizeof(C);
   for (int l = tid * PER; l < M; l += T * PER)
     cp_async16<R>(&S[PER == 2 ? swz(l) : l], st + l);

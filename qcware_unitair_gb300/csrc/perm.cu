@@ -46,7 +46,7 @@ __device__ __forceinline__ int perm_swz(int l) {
 }
 
 template <typename R>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2)
     permute_kernel(const Cx<R>* in, Cx<R>* out, PermArgs a) {
   using C = Cx<R>;
   __shared__ C S[1 << PERM_MAX_TB];
@@ -78,22 +78,53 @@ __global__ void __launch_bounds__(256)
     woff[k] = wo;
     wsm[k] = perm_swz<R>(ls);
   }
-  const int nrest = a.n - a.tb;
-  for (uint64_t t = blockIdx.x; t < a.total_tiles; t += gridDim.x) {
+  // tile t's base offsets: bit j of its index within the state goes to
+  // input bit rest_in[j] and output bit rest_out[j]; lane l handles bits l
+  // and l + 32, an OR over the warp assembles the offsets
+  const int lane = tid & 31, nrest = a.n - a.tb;
+  const uint64_t in0 = lane < nrest ? uint64_t(1) << a.rest_in[lane] : 0;
+  const uint64_t out0 = lane < nrest ? uint64_t(1) << a.rest_out[lane] : 0;
+  const uint64_t in1 =
+      lane + 32 < nrest ? uint64_t(1) << a.rest_in[lane + 32] : 0;
+  const uint64_t out1 =
+      lane + 32 < nrest ? uint64_t(1) << a.rest_out[lane + 32] : 0;
+  auto bases = [&](uint64_t t, uint64_t* bin, uint64_t* bout) {
     const uint64_t s = t / a.tiles_per_state, r = t % a.tiles_per_state;
-    uint64_t bin = 0, bout = 0;
-    for (uint64_t x = r; x; x &= x - 1) {  // set bits only
-      const int j = __ffsll((long long)x) - 1;
-      bin |= uint64_t(1) << a.rest_in[j];
-      bout |= uint64_t(1) << a.rest_out[j];
-    }
-    (void)nrest;
-    const C* src = in + (s << a.n) + bin;
-    C* dst = out + (s << a.n) + bout;
+    const uint64_t i = (((r >> lane) & 1) ? in0 : 0) |
+                       (((r >> (lane + 32)) & 1) ? in1 : 0);
+    const uint64_t o = (((r >> lane) & 1) ? out0 : 0) |
+                       (((r >> (lane + 32)) & 1) ? out1 : 0);
+    *bin = (s << a.n) |
+           ((uint64_t)__reduce_or_sync(0xffffffffu, (unsigned)(i >> 32))
+            << 32) |
+           __reduce_or_sync(0xffffffffu, (unsigned)i);
+    *bout = (s << a.n) |
+            ((uint64_t)__reduce_or_sync(0xffffffffu, (unsigned)(o >> 32))
+             << 32) |
+            __reduce_or_sync(0xffffffffu, (unsigned)o);
+  };
+  uint64_t t = blockIdx.x;
+  if (t >= a.total_tiles) return;
+  // the next tile's loads are issued before the current tile's stores
+  C v[8];
+  uint64_t bin, bout;
+  bases(t, &bin, &bout);
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+    if (k < K) v[k] = __ldcs(in + bin + roff[k]);
+  for (; t < a.total_tiles; t += gridDim.x) {
 #pragma unroll
     for (int k = 0; k < 8; ++k)
-      if (k < K) S[rl[k]] = __ldcs(src + roff[k]);
+      if (k < K) S[rl[k]] = v[k];
     __syncthreads();
+    C* dst = out + bout;
+    const uint64_t nt = t + gridDim.x;
+    if (nt < a.total_tiles) {
+      bases(nt, &bin, &bout);
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        if (k < K) v[k] = __ldcs(in + bin + roff[k]);
+    }
 #pragma unroll
     for (int k = 0; k < 8; ++k)
       if (k < K) __stcs(dst + woff[k], S[wsm[k]]);
