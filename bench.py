@@ -683,12 +683,20 @@ def run_gpu(args, ws, rank, local):
     del psi
     torch.cuda.empty_cache()
 
-    def e2e_step():
+    def e2e_step(ev=None):
+        if ev is not None:
+            ev[0].record()
         state = host_in.to(dev, non_blocking=True)
         ops = [m.to(dev, non_blocking=True) for m in mats_pinned]
+        if ev is not None:
+            ev[1].record()
         for g, m in zip(gates, ops):
             state = ug.apply_operator(m, g.qubits, state)
+        if ev is not None:
+            ev[2].record()
         host_out.copy_(state, non_blocking=True)
+        if ev is not None:
+            ev[3].record()
         return state
 
     e2e_step()
@@ -697,12 +705,20 @@ def run_gpu(args, ws, rank, local):
     e2e_steps = max(1, min(args.steps, 2))
     gc.collect()
     gc.disable()  # no collector pauses inside the timed host loop
+    e2e_ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)]
+              for _ in range(e2e_steps)]
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_step()
+    for k in range(e2e_steps):
+        e2e_step(e2e_ev[k])
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0, dev)
     gc.enable()
+    # where an e2e step's time goes (CUDA events on the launching stream)
+    e2e_parts = {
+        name: round(statistics.mean(ev[i].elapsed_time(ev[i + 1])
+                                    for ev in e2e_ev), 2)
+        for i, name in enumerate(("h2d_ms", "gates_ms", "d2h_ms"))}
+    e2e_parts["wall_ms"] = round(1e3 * e2e_s / e2e_steps, 2)
     e2e_value = bytes_per_gate * G * e2e_steps * ws / e2e_s / 1e9
     h2d = N * 8 + sum(m.numel() * 8 for m in mats_host)
     d2h = N * 8
@@ -741,6 +757,7 @@ def run_gpu(args, ws, rank, local):
         "e2e": {"value": round(e2e_value, 1), "unit": "GB/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "api": "qcware_unitair_gb300.apply_operator (functional)",
+                "step_parts": e2e_parts,
                 "final_norm_drift": drift},
         "fused": {
             "ms_per_step": round(fused_ms, 3), "passes": prog.num_passes,

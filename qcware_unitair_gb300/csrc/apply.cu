@@ -180,8 +180,9 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// k = 3..5 target qubits: one thread per group of 2^k amplitudes.  The
-// thread reads its group once (consecutive threads take consecutive groups,
+// k = 3..5 target qubits: one thread per group of 2^k amplitudes (two
+// groups when one matrix serves all states and both fit in 256 bytes of
+// registers).  The thread reads its group once (consecutive threads take consecutive groups,
 // so every load instruction of a warp is contiguous when bit 0 is not a
 // target), multiplies by the matrix (in shared memory when one matrix
 // serves all states) and writes the group; in place is safe.
@@ -191,7 +192,7 @@ __global__ void __launch_bounds__(128)
                        GenericArgs a) {
   using C = Cx<R>;
   constexpr int D = 1 << K;
-  __shared__ C msm[D * D];
+  __shared__ __align__(16) C msm[D * D];
   __shared__ uint64_t offs[D];
   __shared__ int spos[K];
   const int tid = threadIdx.x;
@@ -219,8 +220,52 @@ __global__ void __launch_bounds__(128)
   const int n = a.n;
   const uint64_t gps = uint64_t(1) << (n - K);  // groups per state
   const uint64_t total = (a.total >> n) * gps;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  auto group_base = [&](uint64_t g, const C** src, C** dst) {
+    const uint64_t s = g / gps;
+    uint64_t base = g % gps;
+#pragma unroll
+    for (int j = 0; j < K; ++j) base = insert_zero(base, spos[j]);
+    *src = in + s * a.in_stride + base;
+    *dst = out + (s << n) + base;
+  };
+  // two groups per thread where their amplitudes fit in registers: every
+  // matrix element read from shared memory feeds both
+  constexpr bool kPair = 2 * D * sizeof(C) <= 256;
+  if constexpr (kPair) {
+    if (shared_op) {
+      for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + tid; g < total;
+           g += 2 * stride) {
+        const uint64_t g1 = g + stride;
+        const bool two = g1 < total;
+        const C *src0, *src1;
+        C *dst0, *dst1;
+        group_base(g, &src0, &dst0);
+        group_base(two ? g1 : g, &src1, &dst1);
+        C x0[D], x1[D];
+#pragma unroll
+        for (int b = 0; b < D; ++b) {
+          x0[b] = src0[offs[b]];
+          x1[b] = src1[offs[b]];
+        }
+#pragma unroll 2
+        for (int r = 0; r < D; ++r) {
+          C acc0 = czero<C>(), acc1 = czero<C>();
+#pragma unroll
+          for (int b = 0; b < D; ++b) {
+            const C mv = msm[r * D + b];
+            acc0 = cmad(mv, x0[b], acc0);
+            acc1 = cmad(mv, x1[b], acc1);
+          }
+          dst0[offs[r]] = acc0;
+          if (two) dst1[offs[r]] = acc1;
+        }
+      }
+      return;
+    }
+  }
   for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + tid; g < total;
-       g += (uint64_t)gridDim.x * blockDim.x) {
+       g += stride) {
     const uint64_t s = g / gps;
     uint64_t base = g % gps;
 #pragma unroll
