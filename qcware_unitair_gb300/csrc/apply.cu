@@ -541,11 +541,43 @@ struct PhaseArgs {
 };
 
 // out = (cos t - i sin t) * psi.
+template <typename RA, typename RS, typename RO>
+__device__ __forceinline__ Cx<RO> phase_one(RA t, Cx<RS> v) {
+  // The phase factor is formed in the angle's precision, as torch forms
+  // exp(-1j * angles) in complex(angles.dtype); the product is then taken
+  // in the promoted output precision.
+  RA sa, ca;
+  sincos(t, &sa, &ca);
+  const RO s = (RO)sa, c = (RO)ca;
+  const RO x = (RO)v.x, y = (RO)v.y;
+  Cx<RO> o;
+  o.x = c * x + s * y;
+  o.y = c * y - s * x;
+  return o;
+}
+
 template <typename RA, typename RS, typename RO, int NDIM>
 __global__ void __launch_bounds__(256)
     phase_kernel(const RA* ang, const Cx<RS>* psi, Cx<RO>* out, PhaseArgs a) {
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-       i < a.total; i += (uint64_t)gridDim.x * blockDim.x) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if constexpr (NDIM == 1) {
+    // four elements per thread, all loads issued before the sincos work
+    const int64_t s0 = a.sa[0], s1 = a.sb[0];
+    for (; i + 3 * stride < a.total; i += 4 * stride) {
+      RA t[4];
+      Cx<RS> v[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        t[k] = ang[(int64_t)(i + k * stride) * s0];
+        v[k] = psi[(int64_t)(i + k * stride) * s1];
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        out[i + k * stride] = phase_one<RA, RS, RO>(t[k], v[k]);
+    }
+  }
+  for (; i < a.total; i += stride) {
     int64_t oa = 0, ob = 0;
     if constexpr (NDIM == 1) {
       oa = (int64_t)i * a.sa[0];
@@ -560,19 +592,7 @@ __global__ void __launch_bounds__(256)
         ob += (int64_t)idx * a.sb[d];
       }
     }
-    // The phase factor is formed in the angle's precision, as torch forms
-    // exp(-1j * angles) in complex(angles.dtype); the product is then taken
-    // in the promoted output precision.
-    const RA t = ang[oa];
-    const Cx<RS> v = psi[ob];
-    RA sa, ca;
-    sincos(t, &sa, &ca);
-    const RO s = (RO)sa, c = (RO)ca;
-    const RO x = (RO)v.x, y = (RO)v.y;
-    Cx<RO> o;
-    o.x = c * x + s * y;
-    o.y = c * y - s * x;
-    out[i] = o;
+    out[i] = phase_one<RA, RS, RO>(ang[oa], psi[ob]);
   }
 }
 

@@ -37,10 +37,13 @@ struct Plan {
   int64_t part_len;
 };
 
-static Plan make_plan(int64_t rows, int64_t dim) {
+// blocks_per_sm: the launching kernel's resident blocks per SM, so that a
+// single row splits into one wave; 16 (the most any reduction kernel keeps
+// resident) gives the largest split, which sizes the scratch
+static Plan make_plan(int64_t rows, int64_t dim, int blocks_per_sm = 16) {
   Plan p{1, dim};
   if (rows <= 0 || dim <= 0) return p;
-  const int64_t want_blocks = (int64_t)sm_count() * 16;
+  const int64_t want_blocks = (int64_t)sm_count() * blocks_per_sm;
   const int64_t min_len = 8192;
   if (rows >= want_blocks || dim <= min_len) return p;
   int64_t parts = (want_blocks + rows - 1) / rows;
@@ -54,6 +57,18 @@ static Plan make_plan(int64_t rows, int64_t dim) {
   p.parts = (int)parts;
   p.part_len = len;
   return p;
+}
+
+// Resident blocks per SM of a RED_THREADS-thread reduction kernel (1..16).
+template <typename Kernel>
+static int resident_blocks(Kernel kernel) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, RED_THREADS,
+                                                    0) != cudaSuccess) {
+    (void)cudaGetLastError();
+    nb = 16;
+  }
+  return nb < 1 ? 1 : (nb > 16 ? 16 : nb);
 }
 
 __device__ __forceinline__ void row_offsets(const RowArgs& a, int64_t row,
@@ -117,14 +132,32 @@ __global__ void __launch_bounds__(RED_THREADS)
   const Cx<R>* p = psi + row * dim;
   Acc<R> acc;
   int64_t i = lo + threadIdx.x;
-  for (; i + 3 * RED_THREADS < hi; i += 4 * RED_THREADS) {
-    Cx<R> v[4];
+  // four elements per step; the next step's loads are in flight while this
+  // step's sums run
+  Cx<R> v[4];
+  bool have = i + 3 * RED_THREADS < hi;
+  if (have) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) v[k] = __ldcs(p + i + k * RED_THREADS);
+  }
+  while (have) {
+    const int64_t ni = i + 4 * RED_THREADS;
+    const bool next = ni + 3 * RED_THREADS < hi;
+    Cx<R> vn[4];
+    if (next) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) vn[k] = __ldcs(p + ni + k * RED_THREADS);
+    }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       acc.add_prod(v[k].x, v[k].x);
       acc.add_prod(v[k].y, v[k].y);
+    }
+    i = ni;
+    have = next;
+    if (next) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) v[k] = vn[k];
     }
   }
   for (; i < hi; i += RED_THREADS) {
@@ -192,16 +225,34 @@ __global__ void __launch_bounds__(RED_THREADS)
     y.add_prod(-u.y, v.x);
   };
   int64_t i = lo + threadIdx.x;
-  // four elements of each input in flight per thread
-  for (; i + 3 * RED_THREADS < hi; i += 4 * RED_THREADS) {
-    Cx<R> u[4], v[4];
+  // four elements of each input per step; the next step's loads are in
+  // flight while this step's sums run
+  auto load4 = [&](int64_t j, Cx<R>* u, Cx<R>* v) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      u[k] = __ldcs(a + oa + (i + k * RED_THREADS) * ra.ia);
-      v[k] = __ldcs(b + ob + (i + k * RED_THREADS) * ra.ib);
+      u[k] = __ldcs(a + oa + (j + k * RED_THREADS) * ra.ia);
+      v[k] = __ldcs(b + ob + (j + k * RED_THREADS) * ra.ib);
     }
+  };
+  Cx<R> u[4], v[4];
+  bool have = i + 3 * RED_THREADS < hi;
+  if (have) load4(i, u, v);
+  while (have) {
+    const int64_t ni = i + 4 * RED_THREADS;
+    const bool next = ni + 3 * RED_THREADS < hi;
+    Cx<R> un[4], vn[4];
+    if (next) load4(ni, un, vn);
 #pragma unroll
     for (int k = 0; k < 4; ++k) step(u[k], v[k]);
+    i = ni;
+    have = next;
+    if (next) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        u[k] = un[k];
+        v[k] = vn[k];
+      }
+    }
   }
   for (; i < hi; i += RED_THREADS)
     step(a[oa + i * ra.ia], b[ob + i * ra.ib]);
@@ -362,7 +413,10 @@ extern "C" int gbsv_norm_squared(const void* state, int dtype,
   if (num_rows == 0) return GBSV_OK;
   if (!out || (dim > 0 && !state))
     return set_error(GBSV_ERR_INVALID_ARG, "null pointer");
-  const Plan p = make_plan(num_rows, dim);
+  static const int nb_f = resident_blocks(norm2_kernel<float>);
+  static const int nb_d = resident_blocks(norm2_kernel<double>);
+  const Plan p =
+      make_plan(num_rows, dim, dtype == GBSV_C64 ? nb_f : nb_d);
   int rc = check_scratch(p, num_rows, 0, scratch, scratch_bytes);
   if (!rc) rc = check_grid(p, num_rows);
   if (rc) return rc;
@@ -418,7 +472,9 @@ extern "C" int gbsv_inner_product(const void* a, const void* b, int dtype,
   if (ra.rows == 0) return GBSV_OK;
   if (!out || (dim > 0 && (!a || !b)))
     return set_error(GBSV_ERR_INVALID_ARG, "null pointer");
-  const Plan p = make_plan(ra.rows, dim);
+  static const int nb_f = resident_blocks(inner_kernel<float>);
+  static const int nb_d = resident_blocks(inner_kernel<double>);
+  const Plan p = make_plan(ra.rows, dim, dtype == GBSV_C64 ? nb_f : nb_d);
   ra.parts = p.parts;
   ra.part_len = p.part_len;
   rc = check_scratch(p, ra.rows, 1, scratch, scratch_bytes);
