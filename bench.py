@@ -472,7 +472,7 @@ def bench_path_rows(dev, n=30):
          lambda: ug.diag_expectation_value(diag, psi), 12, 1),
         ("apply_all_qubits(H)", lambda: ug.apply_all_qubits(h, psi), 16, n),
         ("apply_operator(3 qubits)",
-         lambda: ug.apply_operator(u3, [3, 14, 27], psi), 16, 1),
+         lambda: ug.apply_operator(u3, [3, 14, n - 3], psi), 16, 1),
     ]
     out = {}
     for name, fn, bpa, passes in cases:
@@ -482,7 +482,7 @@ def bench_path_rows(dev, n=30):
                      "GB_s": round(gbs, 1),
                      "frac_of_peak": round(gbs / peak, 3)}
         torch.cuda.empty_cache()
-    return {"workload": f"{n}-qubit complex64 state (8 GiB), functional API",
+    return {"workload": f"{n}-qubit complex64 state ({8 * 2 ** n / 2 ** 30:g} GiB), functional API",
             "peak_GBs": peak, "ops": out}
 
 
@@ -513,7 +513,7 @@ def bench_next_rows(dev, n=30):
                          device=dev)
     perm = list(reversed(range(n)))
     cases = [
-        ("swap(0, 29)", lambda: ug.swap(psi, (0, n - 1)), 16),
+        (f"swap(0, {n - 1})", lambda: ug.swap(psi, (0, n - 1)), 16),
         ("permute_qubits(reversed)", lambda: ug.permute_qubits(perm, psi), 16),
         ("roll_qubits(1)", lambda: ug.roll_qubits(psi, 1), 16),
         ("multi_cz(10 pairs)", lambda: ug.multi_cz(pairs, psi), 16),
@@ -545,7 +545,7 @@ def bench_next_rows(dev, n=30):
                                                (ms / 1e3) / 1e9, 1)})
         out[name] = row
         torch.cuda.empty_cache()
-    return {"workload": f"{n}-qubit complex64 state (8 GiB), functional API",
+    return {"workload": f"{n}-qubit complex64 state ({8 * 2 ** n / 2 ** 30:g} GiB), functional API",
             "peak_GBs": peak, "ops": out}
 
 
