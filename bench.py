@@ -549,6 +549,56 @@ def bench_next_rows(dev, n=30):
             "peak_GBs": peak, "ops": out}
 
 
+# ------------------------------------------------- C1 in complex128 -------
+def bench_c1_c128(dev, n=28, num_gates=1000, seed=0):
+    """The canonical random circuit (1000 gates, numpy seed 0) on a 28-qubit
+    complex128 state (4 GiB, far above L2) from |0...0>: one kernel per gate
+    in place, and as fused stages.  Algorithmic bytes per gate: one read and
+    one write of the state (2 * 2^n * 16 B); a stage counts as one pass.
+    Also the largest amplitude difference between the two paths and the
+    norm drift of the fused result."""
+    import torch
+    import qcware_unitair_gb300 as ug
+    from qcware_unitair_gb300.circuits import random_circuit
+    from qcware_unitair_gb300.fusion import Circuit
+    gates = random_circuit(n, num_gates, seed=seed)
+    mats = [torch.from_numpy(g.matrix()).to(dev) for g in gates]
+    N = 2 ** n
+    psi = torch.zeros(N, dtype=torch.complex128, device=dev)
+
+    def plain():
+        psi.zero_()
+        psi[0] = 1
+        for g, m in zip(gates, mats):
+            ug.apply_operator_(m, g.qubits, psi)
+
+    prog = Circuit.from_gates(n, gates).compile(torch.complex128, dev)
+
+    def fused():
+        psi.zero_()
+        psi[0] = 1
+        prog.run(psi, inplace=True)
+
+    plain_ms = _cuda_time(plain, 1)
+    ref = psi.clone()
+    fused_ms = _cuda_time(fused, 2)
+    diff = float((psi - ref).abs().max())
+    drift = abs(float(torch.linalg.vector_norm(psi)) ** 2 - 1.0)
+    del ref
+    gate_bytes = 2 * N * 16
+    return {"workload": f"{n} qubits complex128 (4 GiB), {num_gates} random "
+                        "gates from |0...0>, in place",
+            "plain_ms": round(plain_ms, 1),
+            "plain_GBs_per_gate": round(gate_bytes * num_gates /
+                                        (plain_ms / 1e3) / 1e9, 1),
+            "fused_ms": round(fused_ms, 1), "passes": prog.num_passes,
+            "fused_hbm_GBs": round(gate_bytes * prog.num_passes /
+                                   (fused_ms / 1e3) / 1e9, 1),
+            "speedup": round(plain_ms / fused_ms, 2),
+            "max_abs_diff_fused_vs_plain": diff,
+            "fused_norm_drift": drift}
+
+
 # ---------------------------------------------------------------- serving --
 def bench_serving(dev, num=300, rate=150.0, qubits=(10, 22)):
     """The serving trace (Poisson arrivals; qubits, depth 20-500 and 1-64
@@ -574,6 +624,26 @@ def bench_serving(dev, num=300, rate=150.0, qubits=(10, 22)):
             "throughput_ratio": round(server["circuits_per_s"] /
                                       plain["circuits_per_s"], 2),
             "p99_ratio": round(plain["p99_s"] / server["p99_s"], 2)}
+
+
+def bench_serving_sweep(dev, rates=(300.0, 600.0), num=300,
+                        wide=(100, 100.0)):
+    """The server alone at higher offered rates (same trace shape, qubits
+    U{10..22}), and a trace over the full qubit range U{10..28} (up to
+    64 x 2^28 amplitudes, 128 GiB, per request) at a lower rate."""
+    from qcware_unitair_gb300.serve import Server, make_trace, summarize
+    out = {}
+    for r in rates:
+        trace = make_trace(num, rate=r, seed=1, qubits=(10, 22))
+        out[f"rate_{r:g}"] = summarize(Server(dev).serve(trace))
+    wn, wr = wide
+    trace = make_trace(wn, rate=wr, seed=2, qubits=(10, 28))
+    out[f"qubits_10_28_rate_{wr:g}"] = summarize(Server(dev).serve(trace))
+    out["workload"] = (f"server only; {num} requests per rate, qubits "
+                       f"U{{10..22}}; {wn} requests at {wr:g}/s with qubits "
+                       "U{10..28}; depth U{20..500}, states U{1..64}, 20% "
+                       "adjoint gradients")
+    return out
 
 
 # -------------------------------------------------------------- GPU arm ---
@@ -784,6 +854,13 @@ def run_gpu(args, ws, rank, local):
         result["next_rows_30q"] = bench_next_rows(dev)
         result["adjoint"] = bench_adjoint(dev)
         result["serving"] = bench_serving(dev)
+        for key, fn in (("serving_sweep", bench_serving_sweep),
+                        ("c1_28q_c128", bench_c1_c128)):
+            torch.cuda.empty_cache()
+            try:
+                result[key] = fn(dev)
+            except Exception as e:  # an extra never loses the line
+                result[key] = {"error": f"{type(e).__name__}: {e}"[:300]}
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_sample(n, gates, args.cpu_seconds)
     if rank == 0:

@@ -68,10 +68,259 @@ __device__ __forceinline__ void apply_regs(C* r, const C* m) {
   }
 }
 
+// complex128: GB300 issues FP64 at a small fraction of its FP32 rate, so a
+// gate's FP64 work, not HBM, bounded the complex128 path.  The matrix's
+// kind (permutation, diagonal, anti-diagonal, real, real diagonal with
+// imaginary off-diagonal, controlled 2x2, general) is found once per thread
+// and each kind runs its own loop with only the FP64 operations it needs.
+// The kind is the same for a whole warp when the operator is shared, and
+// the loops are too large to be turned into selects, so no FP64 work is
+// issued for the other kinds.  Roundings are those of cmul / cmad.
+constexpr int EC_ZERO = 0, EC_ONE = 1, EC_REAL = 2, EC_IMAG = 3,
+              EC_FULL = 4;
+
+// From the bit patterns (integer compares: an FP64 compare costs an FP64
+// issue slot; +0 and -0 are both zero)
+template <typename C>
+__device__ __forceinline__ int entry_class(const C& m) {
+  const unsigned long long xb = __double_as_longlong(m.x);
+  const unsigned long long yb = __double_as_longlong(m.y);
+  const bool xz = (xb << 1) == 0, yz = (yb << 1) == 0;
+  if (yz) return xz ? EC_ZERO : (xb == 0x3FF0000000000000ull ? EC_ONE : EC_REAL);
+  return xz ? EC_IMAG : EC_FULL;
+}
+
+// r[i] *= m for the registers i with (i & MASK) == PAT
+template <typename C, int NR, int MASK, int PAT>
+__device__ __forceinline__ void scale_sel(C* r, const C& m, int cls) {
+  switch (cls) {
+    case EC_ONE:
+      return;
+    case EC_ZERO:
+#pragma unroll
+      for (int i = 0; i < NR; ++i)
+        if ((i & MASK) == PAT) r[i].x = r[i].y = 0;
+      return;
+    case EC_REAL:
+#pragma unroll
+      for (int i = 0; i < NR; ++i)
+        if ((i & MASK) == PAT) {
+          r[i].x = m.x * r[i].x;
+          r[i].y = m.x * r[i].y;
+        }
+      return;
+    case EC_IMAG:
+#pragma unroll
+      for (int i = 0; i < NR; ++i)
+        if ((i & MASK) == PAT) {
+          const C t = r[i];
+          r[i].x = -(m.y * t.y);
+          r[i].y = m.y * t.x;
+        }
+      return;
+    default:
+#pragma unroll
+      for (int i = 0; i < NR; ++i)
+        if ((i & MASK) == PAT) r[i] = cmul(m, r[i]);
+      return;
+  }
+}
+
+constexpr int K1_PERM = 0, K1_DIAG = 1, K1_ANTI = 2, K1_REAL = 3,
+              K1_RX = 4, K1_FULL = 5;
+
+__device__ __forceinline__ int kind_2x2(int c0, int c1, int c2, int c3) {
+  if (c1 == EC_ZERO && c2 == EC_ZERO) return K1_DIAG;
+  if (c0 == EC_ZERO && c3 == EC_ZERO)
+    return c1 == EC_ONE && c2 == EC_ONE ? K1_PERM : K1_ANTI;
+  const bool re = c0 <= EC_REAL && c1 <= EC_REAL && c2 <= EC_REAL &&
+                  c3 <= EC_REAL;
+  if (re) return K1_REAL;
+  if (c0 <= EC_REAL && c3 <= EC_REAL && c1 == EC_IMAG && c2 == EC_IMAG)
+    return K1_RX;
+  return K1_FULL;
+}
+
+// The 2x2 (m0 m1; m2 m3) on register bit T, for the registers i with
+// (i & CM) == CV (a control pattern; 0, 0 for none).
+template <typename C, int NR, int T, int CM, int CV>
+__device__ __forceinline__ void apply_2x2(C* r, const C& m0, const C& m1,
+                                          const C& m2, const C& m3, int kind,
+                                          int c0, int c3) {
+  constexpr int B = 1 << T;
+  switch (kind) {
+    case K1_PERM:
+#pragma unroll
+      for (int i = 0; i < NR; ++i) {
+        if ((i & B) || (i & CM) != CV) continue;
+        const C t = r[i];
+        r[i] = r[i | B];
+        r[i | B] = t;
+      }
+      return;
+    case K1_DIAG:
+      scale_sel<C, NR, B | CM, CV>(r, m0, c0);
+      scale_sel<C, NR, B | CM, B | CV>(r, m3, c3);
+      return;
+    case K1_ANTI:
+#pragma unroll
+      for (int i = 0; i < NR; ++i) {
+        if ((i & B) || (i & CM) != CV) continue;
+        const C a0 = r[i], a1 = r[i | B];
+        r[i] = cmul(m1, a1);
+        r[i | B] = cmul(m2, a0);
+      }
+      return;
+    case K1_REAL:
+#pragma unroll
+      for (int i = 0; i < NR; ++i) {
+        if ((i & B) || (i & CM) != CV) continue;
+        const C a0 = r[i], a1 = r[i | B];
+        r[i].x = fma(m1.x, a1.x, m0.x * a0.x);
+        r[i].y = fma(m1.x, a1.y, m0.x * a0.y);
+        r[i | B].x = fma(m3.x, a1.x, m2.x * a0.x);
+        r[i | B].y = fma(m3.x, a1.y, m2.x * a0.y);
+      }
+      return;
+    case K1_RX:
+#pragma unroll
+      for (int i = 0; i < NR; ++i) {
+        if ((i & B) || (i & CM) != CV) continue;
+        const C a0 = r[i], a1 = r[i | B];
+        r[i].x = fma(-m1.y, a1.y, m0.x * a0.x);
+        r[i].y = fma(m1.y, a1.x, m0.x * a0.y);
+        r[i | B].x = fma(m3.x, a1.x, -(m2.y * a0.y));
+        r[i | B].y = fma(m3.x, a1.y, m2.y * a0.x);
+      }
+      return;
+    default:
+#pragma unroll
+      for (int i = 0; i < NR; ++i) {
+        if ((i & B) || (i & CM) != CV) continue;
+        const C a0 = r[i], a1 = r[i | B];
+        r[i] = cmad(m1, a1, cmul(m0, a0));
+        r[i | B] = cmad(m3, a1, cmul(m2, a0));
+      }
+      return;
+  }
+}
+
+// Precomputed structure of a complex128 operator (see apply_c128).
+struct OpKind {
+  int kind;     // K1_* for 2x2; for 4x4: 0 general, 1 permutation,
+                // 2 diagonal, 3 controlled 2x2
+  int sub;      // 4x4 controlled: K1_* of the 2x2 block
+  int c[4];     // classes of the four diagonal (or block) entries
+  int perm;     // 4x4 permutation: source column of row j in bits 2j..2j+1
+};
+
+template <typename C, int K>
+__device__ __forceinline__ OpKind classify_op(const C* m) {
+  OpKind k{};
+  if constexpr (K == 1) {
+    const int c0 = entry_class(m[0]), c1 = entry_class(m[1]),
+              c2 = entry_class(m[2]), c3 = entry_class(m[3]);
+    k.kind = kind_2x2(c0, c1, c2, c3);
+    k.c[0] = c0;
+    k.c[3] = c3;
+    return k;
+  } else {
+    int cl[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) cl[j] = entry_class(m[j]);
+    bool diag = true, perm = true, ctrl = true;
+    int pm = 0;
+#pragma unroll
+    for (int row = 0; row < 4; ++row) {
+      int ones = 0, nz = 0, col = 0;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int c = cl[4 * row + j];
+        if (c != EC_ZERO) {
+          ++nz;
+          col = j;
+          if (c == EC_ONE) ++ones;
+          if (j != row) diag = false;
+          // controlled: identity on rows 0, 1; rows 2, 3 inside cols 2, 3
+          if (row < 2 ? (j != row || c != EC_ONE) : j < 2) ctrl = false;
+        } else if (row < 2 && j == row) {
+          ctrl = false;
+        }
+      }
+      if (!(nz == 1 && ones == 1)) perm = false;
+      pm |= col << (2 * row);
+    }
+    if (perm) {
+      k.kind = 1;
+      k.perm = pm;
+    } else if (diag) {
+      k.kind = 2;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) k.c[j] = cl[5 * j];
+    } else if (ctrl) {
+      k.kind = 3;
+      k.sub = kind_2x2(cl[10], cl[11], cl[14], cl[15]);
+      k.c[0] = cl[10];
+      k.c[3] = cl[15];
+    } else {
+      k.kind = 0;
+    }
+    return k;
+  }
+}
+
+template <typename C>
+__device__ __forceinline__ C pick4(const C* v, int j) {
+  const C lo = (j & 1) ? v[1] : v[0];
+  const C hi = (j & 1) ? v[3] : v[2];
+  return (j & 2) ? hi : lo;
+}
+
+// Matrix index bit 1 (K = 2: the first target) is register bit RB0, bit 0
+// register bit RB1.
+template <typename C, int NR, int K, int RB0, int RB1>
+__device__ __forceinline__ void apply_c128(C* r, const C* m,
+                                           const OpKind& k) {
+  if constexpr (K == 1) {
+    apply_2x2<C, NR, RB0, 0, 0>(r, m[0], m[1], m[2], m[3], k.kind, k.c[0],
+                                k.c[3]);
+  } else {
+    constexpr int M0 = 1 << RB0, M1 = 1 << RB1;
+    switch (k.kind) {
+      case 1:  // permutation: row j takes column perm_j
+#pragma unroll
+        for (int i = 0; i < NR; ++i) {
+          if (i & (M0 | M1)) continue;
+          const int idx[4] = {i, i | M1, i | M0, i | M0 | M1};
+          C v[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) v[j] = r[idx[j]];
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            r[idx[j]] = pick4(v, (k.perm >> (2 * j)) & 3);
+        }
+        return;
+      case 2:  // diagonal
+        scale_sel<C, NR, M0 | M1, 0>(r, m[0], k.c[0]);
+        scale_sel<C, NR, M0 | M1, M1>(r, m[5], k.c[1]);
+        scale_sel<C, NR, M0 | M1, M0>(r, m[10], k.c[2]);
+        scale_sel<C, NR, M0 | M1, M0 | M1>(r, m[15], k.c[3]);
+        return;
+      case 3:  // controlled: the lower-right 2x2 where bit RB0 is set
+        apply_2x2<C, NR, RB1, M0, M0>(r, m[10], m[11], m[14], m[15], k.sub,
+                                      k.c[0], k.c[3]);
+        return;
+      default:
+        apply_regs<C, NR, K, RB0, RB1>(r, m);
+        return;
+    }
+  }
+}
+
 // NH high targets (chunks per unit = 2^NH); RB0 / RB1 are the register-index
 // bits of the first / second target in matrix order.
 template <typename R, int V, int K, int NH, int RB0, int RB1>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
     dense_chunk_kernel(const Cx<R>* in, Cx<R>* out, const Cx<R>* ops,
                        DenseArgs a) {
   using C = Cx<R>;
@@ -82,6 +331,8 @@ __global__ void __launch_bounds__(256)
   constexpr int UNROLL = NR >= TARGET ? 1 : TARGET / NR;
 
   C m[D * D];
+  OpKind kind{};  // complex128: the operator's structure
+  constexpr bool kClassed = sizeof(R) == 8;
   const bool shared_op = a.op_stride == 0;
   if (shared_op) {
 #pragma unroll
@@ -115,6 +366,16 @@ __global__ void __launch_bounds__(256)
     }
   }
 
+  // complex128 with a shared operator: classified while the state loads
+  // are in flight, then one structured pass over every unit's registers
+  // (the target bits index within each unit's NR block; registers of units
+  // past the end are computed and not stored)
+  if constexpr (kClassed) {
+    if (shared_op) {
+      kind = classify_op<C, K>(m);
+      apply_c128<C, UNROLL * NR, K, RB0, RB1>(&reg[0][0], m, kind);
+    }
+  }
 #pragma unroll
   for (int u = 0; u < UNROLL; ++u) {
     const uint64_t g = first + (uint64_t)u * blockDim.x;
@@ -123,8 +384,10 @@ __global__ void __launch_bounds__(256)
       const C* mp = ops + state[u] * a.op_stride;
 #pragma unroll
       for (int j = 0; j < D * D; ++j) m[j] = __ldg(mp + j);
+      apply_regs<C, NR, K, RB0, RB1>(reg[u], m);
+    } else if constexpr (!kClassed) {
+      apply_regs<C, NR, K, RB0, RB1>(reg[u], m);
     }
-    apply_regs<C, NR, K, RB0, RB1>(reg[u], m);
     C* dst = out + obase[u];
 #pragma unroll
     for (int c = 0; c < NCH; ++c) {

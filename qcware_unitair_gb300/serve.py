@@ -9,7 +9,11 @@ the GPU:
               fits the byte budget (160 GB by default).  If the head of the
               queue does not fit, later requests may pass it only until it
               has waited ``reserve_after`` seconds; from then on admission
-              waits for memory, so large requests are not starved.
+              waits for memory, so large requests are not starved.  A
+              request larger than the whole budget (up to 64 x 2^28
+              amplitudes with gradients) is split at arrival into parts of
+              whole 8-state blocks that fit; their outputs are joined in
+              state order when the last part finishes.
   packing     admitted requests whose states fit one tile (n <= 13 for
               complex64) are packed, whatever their circuits, into ONE
               multi-program launch per qubit count (gbsv_run_programs: one
@@ -27,6 +31,7 @@ request with arrival, admission and completion times.
 from __future__ import annotations
 
 import collections
+import dataclasses
 import math
 import time
 from dataclasses import dataclass, field
@@ -40,6 +45,13 @@ from .circuits import Gate, gate_matrix, random_circuit, ROTATIONS
 from .fusion import (FG_DTYPE, Program, gate_list_desc, native_plan)
 
 
+# States are drawn in blocks of STATE_BLOCK, block b from its own generator
+# seeded by (request seed, b), so any run of whole blocks of a request can be
+# generated on its own: a request too large for the HBM budget is served as
+# parts of whole blocks that reproduce the unsplit request's states.
+STATE_BLOCK = 8
+
+
 @dataclass
 class Request:
     rid: int
@@ -49,15 +61,33 @@ class Request:
     gates: List[Gate]
     want_grad: bool = False
     seed: int = 0
+    state_offset: int = 0  # first state of this part (a multiple of 8)
 
     @property
     def state_bytes(self) -> int:
         return self.num_states * (8 << self.num_qubits)
 
     @property
+    def bytes_per_state(self) -> int:
+        # gradients keep psi, two copies for the sweep, lambda and its
+        # buffer
+        return (8 << self.num_qubits) * (6 if self.want_grad else 1)
+
+    @property
     def footprint(self) -> int:
-        # gradients keep psi, lambda and up to ~sqrt(depth) checkpoints
-        return self.state_bytes * (6 if self.want_grad else 1)
+        return self.num_states * self.bytes_per_state
+
+    def split(self, budget: float) -> List["Request"]:
+        """Parts of whole state blocks whose footprints fit ``budget`` (the
+        request itself when it fits, or when one block does not)."""
+        per_block = STATE_BLOCK * self.bytes_per_state
+        if self.footprint <= budget or per_block > budget:
+            return [self]
+        step = int(budget // per_block) * STATE_BLOCK
+        return [dataclasses.replace(self, num_states=min(step,
+                                                         self.num_states - k),
+                                    state_offset=self.state_offset + k)
+                for k in range(0, self.num_states, step)]
 
 
 @dataclass
@@ -109,10 +139,20 @@ def summarize(results: Sequence[Result]) -> dict:
 
 # ---------------------------------------------------------------- helpers --
 def _init_states(req: Request, device, dtype=torch.complex64):
+    """The request's states [state_offset, state_offset + num_states):
+    standard-normal amplitudes, normalised per state, block by block."""
+    N = 2 ** req.num_qubits
+    psi = torch.empty(req.num_states, N, dtype=dtype, device=device)
     g = torch.Generator(device=device)
-    g.manual_seed(int(req.seed))
-    psi = torch.randn(req.num_states, 2 ** req.num_qubits, dtype=dtype,
-                      device=device, generator=g)
+    first = req.state_offset
+    end = first + req.num_states
+    for b in range(first // STATE_BLOCK, (end - 1) // STATE_BLOCK + 1):
+        lo, hi = b * STATE_BLOCK, min((b + 1) * STATE_BLOCK, end)
+        g.manual_seed((int(req.seed) * 0x9E3779B1 + b) & ((1 << 62) - 1))
+        blk = torch.randn(hi - lo, N, dtype=dtype, device=device,
+                          generator=g)
+        a = max(lo, first)
+        psi[a - first:hi - first] = blk[a - lo:]
     psi /= states.norm_squared(psi).sqrt().unsqueeze(-1)
     return psi
 
@@ -177,6 +217,20 @@ def _run_grad(req: Request, psi0: torch.Tensor, fuse: bool = True):
                            fuse=fuse).run(psi, inplace=True)
     sweep = _backward_fused if fuse else _backward_sweep
     return sweep(pc, params, H, psi, [], torch.complex64)
+
+
+def _merge_parts(done_parts) -> Result:
+    """One Result from the Results of a split request's parts: outputs
+    concatenated in state order, admitted at the first part's admission,
+    done when the last part is."""
+    rs = [r for _, r in sorted(done_parts, key=lambda x: x[0])]
+    grads = (np.concatenate([r.grads for r in rs])
+             if rs[0].grads is not None else None)
+    final = (torch.cat([r.final for r in rs])
+             if all(r.final is not None for r in rs) else None)
+    return Result(rs[0].rid, np.concatenate([r.norms for r in rs]),
+                  np.concatenate([r.z0 for r in rs]), grads, rs[0].arrival,
+                  min(r.admitted for r in rs), max(r.done for r in rs), final)
 
 
 # ----------------------------------------------------------------- server --
@@ -276,6 +330,7 @@ class Server:
         waiting: collections.deque = collections.deque()
         inflight = []
         results: Dict[int, Result] = {}
+        parts: Dict[int, list] = {}  # rid -> [parts left, finished parts]
         admitted_at = {}
         used = 0.0
         t0 = time.perf_counter()
@@ -286,7 +341,11 @@ class Server:
         while pending or waiting or inflight:
             now = clock()
             while pending and pending[0].arrival <= now:
-                waiting.append(pending.popleft())
+                req = pending.popleft()
+                split = req.split(self.budget)
+                if len(split) > 1:
+                    parts[req.rid] = [len(split), []]
+                waiting.extend(split)
             # admission
             small, large = [], []
             blocked = False
@@ -297,7 +356,7 @@ class Server:
                     waiting.remove(req)
                     used += req.footprint
                     self.peak_used = max(self.peak_used, used)
-                    admitted_at[req.rid] = now
+                    admitted_at[req.rid, req.state_offset] = now
                     if req.num_qubits <= self.small_max and not req.want_grad:
                         small.append(req)
                     else:
@@ -317,11 +376,20 @@ class Server:
                 ev, req, psi, (norms, z0), grads, _keep = item
                 if ev.query():
                     done = clock()
-                    results[req.rid] = Result(
+                    res = Result(
                         req.rid, norms.cpu().numpy(), z0.cpu().numpy(),
                         grads.cpu().numpy() if grads is not None else None,
-                        req.arrival, admitted_at[req.rid], done,
-                        psi if self.keep_states else None)
+                        req.arrival, admitted_at[req.rid, req.state_offset],
+                        done, psi if self.keep_states else None)
+                    if req.rid in parts:
+                        entry = parts[req.rid]
+                        entry[0] -= 1
+                        entry[1].append((req.state_offset, res))
+                        if entry[0] == 0:
+                            results[req.rid] = _merge_parts(entry[1])
+                            del parts[req.rid]
+                    else:
+                        results[req.rid] = res
                     used -= req.footprint
                 else:
                     still.append(item)

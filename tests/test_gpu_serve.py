@@ -67,3 +67,25 @@ def test_admission_budget_and_overlap():
     assert overlap
     s = summarize(res)
     assert s["requests"] == 30 and s["p99_s"] >= s["p50_s"]
+
+
+def test_oversized_requests_split_by_state_blocks():
+    """With a budget below their footprints, requests run as parts of whole
+    8-state blocks; the joined outputs equal the unsplit requests'."""
+    trace = make_trace(6, rate=1000.0, seed=5, qubits=(12, 15),
+                       depth=(20, 60), batch=(17, 40), grad_fraction=0.5)
+    budget = max(8 * r.bytes_per_state for r in trace)  # a block fits
+    whole = Server(DEV, keep_states=True).serve(trace)
+    srv = Server(DEV, budget_bytes=budget, keep_states=True)
+    split = srv.serve(trace)
+    assert srv.peak_used <= budget
+    assert any(r.footprint > budget for r in trace)
+    for req, a, b in zip(trace, whole, split):
+        assert a.rid == b.rid == req.rid
+        assert b.norms.shape == (req.num_states,)
+        assert np.array_equal(a.final.cpu().numpy(), b.final.cpu().numpy())
+        assert np.abs(a.norms - b.norms).max() <= 1e-12
+        assert np.abs(a.z0 - b.z0).max() <= 1e-12
+        if req.want_grad:
+            assert np.abs(a.grads - b.grads).max() <= 1e-6 * max(
+                1.0, np.abs(a.grads).max())
