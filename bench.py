@@ -646,6 +646,25 @@ def bench_serving_sweep(dev, rates=(300.0, 600.0), num=300,
     return out
 
 
+def _gpu_local_cpus(dev):
+    """CPUs on the GPU's NUMA node (sysfs local_cpulist of its PCI
+    function), or None when unknown."""
+    import torch
+    try:
+        p = torch.cuda.get_device_properties(dev)
+        bdf = (f"{getattr(p, 'pci_domain_id', 0):04x}:"
+               f"{p.pci_bus_id:02x}:{p.pci_device_id:02x}.0")
+        txt = Path(f"/sys/bus/pci/devices/{bdf}/local_cpulist").read_text()
+        cpus = set()
+        for part in txt.strip().split(","):
+            lo, _, hi = part.partition("-")
+            cpus.update(range(int(lo), int(hi or lo) + 1))
+        cpus &= os.sched_getaffinity(0)
+        return cpus or None
+    except (OSError, ValueError, AttributeError, RuntimeError):
+        return None
+
+
 # -------------------------------------------------------------- GPU arm ---
 def run_gpu(args, ws, rank, local):
     import numpy as np
@@ -746,10 +765,19 @@ def run_gpu(args, ws, rank, local):
     stage_ms = fused_ms / prog.num_passes
 
     # ---- e2e through the public functional API, host buffers -----------
-    host_in = torch.zeros(N, dtype=torch.complex64, pin_memory=True)
-    host_in[0] = 1
-    host_out = torch.empty(N, dtype=torch.complex64, pin_memory=True)
-    mats_pinned = [m.pin_memory() for m in mats_host]
+    # pinned buffers are placed from the GPU's local CPUs: pages pinned on
+    # a far NUMA node cut host-to-device bandwidth several-fold
+    cpus = _gpu_local_cpus(dev)
+    old_aff = os.sched_getaffinity(0)
+    if cpus:
+        os.sched_setaffinity(0, cpus)
+    try:
+        host_in = torch.zeros(N, dtype=torch.complex64, pin_memory=True)
+        host_in[0] = 1
+        host_out = torch.zeros(N, dtype=torch.complex64, pin_memory=True)
+        mats_pinned = [m.pin_memory() for m in mats_host]
+    finally:
+        os.sched_setaffinity(0, old_aff)
     del psi
     torch.cuda.empty_cache()
 
