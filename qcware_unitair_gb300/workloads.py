@@ -4,6 +4,7 @@
     python -m qcware_unitair_gb300.workloads gates 24 H 64     # one stage, 64 H
     python -m qcware_unitair_gb300.workloads adjoint 16        # 20q ansatz grad
     python -m qcware_unitair_gb300.workloads serve 300         # server only
+    python -m qcware_unitair_gb300.workloads kinds 28          # c128 per gate
 
 Each runs its workload twice (a warm-up, then a CUDA-event-timed run) and
 prints one line; under a profiler, skip the first run's launches.
@@ -24,6 +25,11 @@ loss mean(<sum Z> + 0.5 <sum XX>).
 10-22 qubits, depth 20-500, 1-64 states, 20% adjoint gradients) replayed
 once against the continuous-batching server after a 16-request warm-up,
 with the host time of the server's launch paths.
+
+``kinds``: one plain gate of each canonical kind (angle 0.7 for rotations)
+applied in place to an n-qubit complex128 state, 10 launches after 2
+warm-up launches each, ms per launch and GB/s over one read and one write
+of the state.
 """
 from __future__ import annotations
 
@@ -147,6 +153,34 @@ def serve(num: int = 300) -> float:
     return res["circuits_per_s"]
 
 
+def kinds(n: int = 28) -> None:
+    import qcware_unitair_gb300 as ug
+    from .circuits import gate_matrix
+    dev = torch.device("cuda")
+    psi = torch.randn(2 ** n, dtype=torch.complex128, device=dev)
+    psi /= psi.abs().pow(2).sum().sqrt()
+    cases = [("X", [5]), ("H", [5]), ("RY", [5]), ("RX", [5]), ("RZ", [5]),
+             ("T", [5]), ("Z", [5]), ("Y", [5]), ("CNOT", [3, 20]),
+             ("CZ", [3, 20]), ("SWAP", [3, 20]), ("X", [n - 1]),
+             ("RX", [n - 1]), ("CNOT", [n - 2, n - 1])]
+    for name, q in cases:
+        theta = 0.7 if name.startswith("R") else None
+        m = torch.from_numpy(gate_matrix(name, theta)).to(dev)
+        for _ in range(2):
+            ug.apply_operator_(m, q, psi)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            ug.apply_operator_(m, q, psi)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 10
+        print(f"kinds n={n} {name} {q}: {ms:.3f} ms "
+              f"{2 * 16 * 2 ** n / ms / 1e6:.0f} GB/s")
+
+
 if __name__ == "__main__":
     what, args = sys.argv[1], sys.argv[2:]
     if what == "stage":
@@ -158,5 +192,7 @@ if __name__ == "__main__":
         adjoint(*(int(a) for a in args))
     elif what == "serve":
         serve(*(int(a) for a in args))
+    elif what == "kinds":
+        kinds(*(int(a) for a in args))
     else:
         raise SystemExit(f"unknown workload {what}")
