@@ -769,15 +769,21 @@ def run_gpu(args, ws, rank, local):
     # a far NUMA node cut host-to-device bandwidth several-fold
     cpus = _gpu_local_cpus(dev)
     old_aff = os.sched_getaffinity(0)
-    if cpus:
-        os.sched_setaffinity(0, cpus)
+    try:
+        if cpus:
+            os.sched_setaffinity(0, cpus)
+    except OSError:
+        pass
     try:
         host_in = torch.zeros(N, dtype=torch.complex64, pin_memory=True)
         host_in[0] = 1
         host_out = torch.zeros(N, dtype=torch.complex64, pin_memory=True)
         mats_pinned = [m.pin_memory() for m in mats_host]
     finally:
-        os.sched_setaffinity(0, old_aff)
+        try:
+            os.sched_setaffinity(0, old_aff)
+        except OSError:
+            pass
     del psi
     torch.cuda.empty_cache()
 
