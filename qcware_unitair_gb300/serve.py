@@ -69,8 +69,8 @@ class Request:
 
     @property
     def bytes_per_state(self) -> int:
-        # gradients keep psi, two copies for the sweep, lambda and its
-        # buffer
+        # gradients: the request's states, the forward copy, psi and lambda
+        # of the sweep, and room for the sweep's temporaries
         return (8 << self.num_qubits) * (6 if self.want_grad else 1)
 
     @property
@@ -312,8 +312,8 @@ class Server:
         with torch.cuda.stream(stream):
             psi = _init_states(req, self.device)
             grads = None
-            if req.want_grad:
-                grads = _run_grad(req, psi.clone())
+            if req.want_grad:  # reads psi (its own forward runs on a copy)
+                grads = _run_grad(req, psi)
             prog = Program.from_gate_list(req.gates, req.num_qubits,
                                           torch.complex64, self.device)
             prog.run(psi, inplace=True)
@@ -415,7 +415,7 @@ def serve_plain(trace: Sequence[Request], device="cuda",
         psi = _init_states(req, dev)
         grads = None
         if req.want_grad:
-            grads = _run_grad(req, psi.clone(), fuse=False)
+            grads = _run_grad(req, psi, fuse=False)
         # all of the request's gate matrices in one transfer, then one
         # kernel per gate
         mats = [torch.from_numpy(g.matrix()) for g in req.gates]
