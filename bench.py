@@ -778,7 +778,17 @@ def run_gpu(args, ws, rank, local):
         host_in = torch.zeros(N, dtype=torch.complex64, pin_memory=True)
         host_in[0] = 1
         host_out = torch.zeros(N, dtype=torch.complex64, pin_memory=True)
-        mats_pinned = [m.pin_memory() for m in mats_host]
+        # the step's gate matrices as one pinned tensor per size (one copy
+        # each instead of a thousand small ones)
+        sizes = sorted({m.shape[-1] for m in mats_host})
+        stacked = {d: torch.stack([m for m in mats_host if m.shape[-1] == d])
+                   .pin_memory() for d in sizes}
+        slot = []
+        seen = {d: 0 for d in sizes}
+        for m in mats_host:
+            d = m.shape[-1]
+            slot.append((d, seen[d]))
+            seen[d] += 1
     finally:
         try:
             os.sched_setaffinity(0, old_aff)
@@ -791,7 +801,8 @@ def run_gpu(args, ws, rank, local):
         if ev is not None:
             ev[0].record()
         state = host_in.to(dev, non_blocking=True)
-        ops = [m.to(dev, non_blocking=True) for m in mats_pinned]
+        dmats = {d: t.to(dev, non_blocking=True) for d, t in stacked.items()}
+        ops = [dmats[d][i] for d, i in slot]
         if ev is not None:
             ev[1].record()
         for g, m in zip(gates, ops):
