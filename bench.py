@@ -655,14 +655,21 @@ def _gpu_local_cpus(dev):
         bdf = (f"{getattr(p, 'pci_domain_id', 0):04x}:"
                f"{p.pci_bus_id:02x}:{p.pci_device_id:02x}.0")
         txt = Path(f"/sys/bus/pci/devices/{bdf}/local_cpulist").read_text()
-        cpus = set()
-        for part in txt.strip().split(","):
-            lo, _, hi = part.partition("-")
-            cpus.update(range(int(lo), int(hi or lo) + 1))
-        cpus &= os.sched_getaffinity(0)
+        cpus = parse_cpulist(txt) & os.sched_getaffinity(0)
         return cpus or None
     except (OSError, ValueError, AttributeError, RuntimeError):
         return None
+
+
+def parse_cpulist(txt: str) -> set:
+    """CPU numbers of a sysfs cpulist such as "0-3,8,10-11"."""
+    cpus = set()
+    for part in txt.strip().split(","):
+        if not part:
+            continue
+        lo, _, hi = part.partition("-")
+        cpus.update(range(int(lo), int(hi or lo) + 1))
+    return cpus
 
 
 # -------------------------------------------------------------- GPU arm ---
