@@ -15,7 +15,7 @@ the hot path.
 from __future__ import annotations
 
 import math
-from typing import Optional, Union
+from typing import Dict, Iterable, Optional, Union
 
 import torch
 
@@ -136,3 +136,17 @@ def cz(device=None, dtype=None):
 def swap(device=None, dtype=None):
     return _const([[1, 0, 0, 0], [0, 0, 1, 0], [0, 1, 0, 0], [0, 0, 0, 1]],
                   device, dtype)
+
+
+def fuse_single_qubit_operators(
+        qubits: Iterable[int],
+        operators: Iterable[torch.Tensor]) -> Dict[int, torch.Tensor]:
+    """Per qubit, the product of the single-qubit operators listed for it,
+    later operators on the left (gates/matrix_algebra.py:6-51): qubits
+    [2, 4, 2, 7] with operators A, B, C, D give {2: C @ A, 4: B, 7: D}.
+    Operators are (*batch, 2, 2) and multiply with torch.matmul's batch
+    broadcasting; keys keep the order of first appearance."""
+    fused: Dict[int, torch.Tensor] = {}
+    for q, op in zip(qubits, operators):
+        fused[q] = torch.matmul(op, fused[q]) if q in fused else op
+    return fused

@@ -471,15 +471,16 @@ def apply_to_qubits(operators: Iterable[torch.Tensor], qubits: Iterable[int],
     (operations.py:416-503).  Operators on the same qubit are multiplied
     first, as unitair does (gates/matrix_algebra.py:6-51); with unbatched
     operators the fused per-qubit gates then run as one fused program."""
+    from .gates import fuse_single_qubit_operators
     n = count_qubits(state)
-    fused: dict = {}
-    for q, op in zip(qubits, operators):
-        q = int(q)
-        if not 0 <= q < n:
+    pairs = list(zip(qubits, operators))
+    for q, _ in pairs:
+        if not 0 <= int(q) < n:
             raise ValueError(
                 "Expected index in {-num_qubits, ..., num_qubits - 1}.\n"
-                f"Num_qubits: {n}, index: {q}.")
-        fused[q] = torch.matmul(op, fused[q]) if q in fused else op
+                f"Num_qubits: {n}, index: {int(q)}.")
+    fused = fuse_single_qubit_operators([int(q) for q, _ in pairs],
+                                        [op for _, op in pairs])
     if not fused:
         return state.contiguous()
     ops = list(fused.items())

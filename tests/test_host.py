@@ -130,3 +130,21 @@ def test_circuit_generator_is_deterministic():
     for g in a:
         assert len(set(g.qubits)) == len(g.qubits)
         assert all(0 <= q < 30 for q in g.qubits)
+
+
+def test_fuse_single_qubit_operators():
+    """Per qubit, later operators multiply on the left
+    (gates/matrix_algebra.py:6-51), with torch batch broadcasting."""
+    from qcware_unitair_gb300.gates import fuse_single_qubit_operators
+    g = torch.Generator().manual_seed(0)
+    A, B, C, D = (torch.randn(2, 2, dtype=torch.complex128, generator=g)
+                  for _ in range(4))
+    out = fuse_single_qubit_operators([2, 4, 2, 7], [A, B, C, D])
+    assert list(out) == [2, 4, 7]
+    assert torch.equal(out[2], C @ A)
+    assert out[4] is B and out[7] is D
+    E = torch.randn(5, 2, 2, dtype=torch.complex128, generator=g)
+    out = fuse_single_qubit_operators(iter([1, 1, 1]), iter([A, E, B]))
+    assert out[1].shape == (5, 2, 2)
+    assert torch.allclose(out[1], B @ (E @ A))
+    assert fuse_single_qubit_operators([], []) == {}
