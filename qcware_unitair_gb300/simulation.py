@@ -25,6 +25,7 @@ from typing import Iterable, Optional, Sequence, Tuple
 import torch
 
 from . import _core, _lib
+from .measurement import measure  # noqa: F401  (unitair.simulation.measure)
 from .states import (count_qubits, count_qubits_gate_matrix,
                      StateShapeError)  # noqa: F401  (re-exported errors)
 

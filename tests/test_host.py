@@ -148,3 +148,31 @@ def test_fuse_single_qubit_operators():
     assert out[1].shape == (5, 2, 2)
     assert torch.allclose(out[1], B @ (E @ A))
     assert fuse_single_qubit_operators([], []) == {}
+
+
+def test_public_names_of_unitair_present():
+    """Every name unitair exports from unitair, unitair.simulation,
+    unitair.states and unitair.gates (their __init__ files) exists here."""
+    from qcware_unitair_gb300 import gates as G
+    sim_names = ["apply_phase", "apply_operator", "apply_to_qubits",
+                 "apply_all_qubits", "act_last_qubit", "swap", "multi_cz",
+                 "multi_controlled_x", "multi_controlled_z",
+                 "act_first_qubits", "measure"]
+    state_names = ["StateLayout", "StateShapeError", "count_qubits",
+                   "count_qubits_tensor", "count_qubits_gate_matrix",
+                   "hilbert_space_dim", "count_batch_dims_tensor",
+                   "subset_roll_to_back", "subset_roll_to_front",
+                   "to_tensor_layout", "to_vector_layout", "inner_product",
+                   "norm_squared", "abs_squared", "diag_expectation_value"]
+    top_names = ["states", "simulation", "StateLayout", "unit_vector",
+                 "uniform_superposition", "rand_state", "count_qubits",
+                 "hilbert_space_dim", "diag_expectation_value",
+                 "inner_product", "norm_squared", "abs_squared",
+                 "VECTOR_LAYOUT", "TENSOR_LAYOUT"]
+    gate_names = ["exp_x", "exp_y", "exp_z", "cnot", "cx", "cz", "hadamard",
+                  "pauli_x", "pauli_y", "pauli_z",
+                  "fuse_single_qubit_operators"]
+    for mod, names in ((sim, sim_names), (S, state_names), (ug, top_names),
+                       (G, gate_names)):
+        missing = [n for n in names if not hasattr(mod, n)]
+        assert not missing, (mod.__name__, missing)
