@@ -39,6 +39,15 @@ _OPERATIONS = {
     "multi_cz": simulation.multi_cz,
     "multi_controlled_z": simulation.multi_controlled_z,
     "multi_controlled_x": simulation.multi_controlled_x,
+    # tensor-layout variants (operations.py:151-654)
+    "apply_operator_tensor": simulation.apply_operator_tensor,
+    "act_first_qubits_tensor": simulation.act_first_qubits_tensor,
+    "act_last_qubit_tensor": simulation.act_last_qubit_tensor,
+    "apply_all_qubits_tensor": simulation.apply_all_qubits_tensor,
+    "apply_to_qubits_tensor": simulation.apply_to_qubits_tensor,
+    "swap_tensor": simulation.swap_tensor,
+    "roll_qubits_tensor": simulation.roll_qubits_tensor,
+    "permute_qubits_tensor": simulation.permute_qubits_tensor,
 }
 _SIM_EXPORTS = ("apply_operator", "apply_all_qubits", "apply_phase",
                 "act_first_qubits", "act_last_qubit", "apply_to_qubits",

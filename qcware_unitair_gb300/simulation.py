@@ -28,6 +28,7 @@ from . import _core, _lib
 from .measurement import measure  # noqa: F401  (unitair.simulation.measure)
 from .states import (count_qubits, count_qubits_gate_matrix,
                      StateShapeError)  # noqa: F401  (re-exported errors)
+from .states import StateLayout, count_batch_dims_tensor, get_qubit_indices
 
 
 # ----------------------------------------------------------------- helpers --
@@ -588,3 +589,134 @@ def multi_controlled_x(state_vector: torch.Tensor, controls: Iterable[int],
             _core.stream_of(s.device))
         _lib.check(rc, "multi_controlled_x")
     return out
+
+
+# ------------------------------------------------- tensor-layout variants --
+# unitair's *_tensor functions take states in tensor layout, (*batch, 2, ...,
+# 2) with one dim per qubit.  That layout is a view of the vector layout, so
+# each variant reshapes to (*batch, 2^n), runs the vector function's kernel
+# and returns the result viewed in tensor layout.  The pure permutations
+# (swap_tensor, roll_qubits_tensor, permute_qubits_tensor without
+# contiguous_output) are views in unitair and stay views here: no data moves.
+def _as_vector(state_tensor: torch.Tensor, num_qubits: int) -> torch.Tensor:
+    if state_tensor.dim() < num_qubits or any(
+            d != 2 for d in state_tensor.shape[state_tensor.dim() -
+                                               num_qubits:]):
+        raise StateShapeError(data=state_tensor,
+                              expected_layout=StateLayout.TENSOR)
+    batch = state_tensor.shape[:state_tensor.dim() - num_qubits]
+    return state_tensor.reshape(batch + torch.Size((2 ** num_qubits,)))
+
+
+def _as_tensor(state: torch.Tensor, num_qubits: int) -> torch.Tensor:
+    return state.view(state.shape[:-1] + torch.Size(num_qubits * [2]))
+
+
+def _check_gate_qubits(operator: torch.Tensor, given: Optional[int]) -> int:
+    k = count_qubits_gate_matrix(operator)
+    if given is not None and int(given) != k:
+        raise ValueError(f"Operator of size {tuple(operator.shape[-2:])} "
+                         f"acts on {k} qubit(s), not {given}.")
+    return k
+
+
+def apply_operator_tensor(operator: torch.Tensor, qubits: Iterable[int],
+                          state_tensor: torch.Tensor, num_qubits: int,
+                          operator_num_qubits: Optional[int] = None
+                          ) -> torch.Tensor:
+    """apply_operator on a state in tensor layout (operations.py:151-186);
+    contiguous result in tensor layout."""
+    _check_gate_qubits(operator, operator_num_qubits)
+    out = apply_operator(operator, list(qubits),
+                         _as_vector(state_tensor, num_qubits))
+    return _as_tensor(out, num_qubits)
+
+
+def act_first_qubits_tensor(operator: torch.Tensor,
+                            state_tensor: torch.Tensor, num_qubits: int,
+                            gate_num_qubits: Optional[int] = None
+                            ) -> torch.Tensor:
+    """A k-qubit operator on qubits 0..k-1 of a tensor-layout state, batch
+    rules as act_first_qubits (operations.py:258-329)."""
+    k = _check_gate_qubits(operator, gate_num_qubits)
+    if num_qubits < k:
+        raise ValueError(f"Attempted to apply a {k}-qubit gate to "
+                         f"{num_qubits} qubit(s).")
+    out = apply_operator(operator, range(k),
+                         _as_vector(state_tensor, num_qubits))
+    return _as_tensor(out, num_qubits)
+
+
+def act_last_qubit_tensor(single_qubit_operator: torch.Tensor,
+                          state_tensor: torch.Tensor) -> torch.Tensor:
+    """A (2, 2) operator contracted with the last dim of the tensor
+    (operations.py:216-233, deprecated in unitair): every length-2 fibre of
+    the last dim is a one-qubit state."""
+    if tuple(single_qubit_operator.shape) != (2, 2):
+        raise ValueError("act_last_qubit_tensor takes one (2, 2) operator, "
+                         f"got {tuple(single_qubit_operator.shape)}.")
+    if state_tensor.dim() < 1 or state_tensor.shape[-1] != 2:
+        raise StateShapeError(data=state_tensor,
+                              expected_layout=StateLayout.TENSOR)
+    out = apply_operator(single_qubit_operator, [0],
+                         state_tensor.reshape(-1, 2))
+    return out.view(state_tensor.shape)
+
+
+def apply_all_qubits_tensor(operator: torch.Tensor,
+                            state_tensor: torch.Tensor,
+                            num_qubits: int) -> torch.Tensor:
+    """apply_all_qubits on a tensor-layout state (operations.py:369-413)."""
+    out = apply_all_qubits(operator, _as_vector(state_tensor, num_qubits))
+    return _as_tensor(out, num_qubits)
+
+
+def apply_to_qubits_tensor(operators: Iterable[torch.Tensor],
+                           qubits: Iterable[int], state_tensor: torch.Tensor,
+                           num_qubits: int) -> torch.Tensor:
+    """apply_to_qubits on a tensor-layout state (operations.py:449-503)."""
+    out = apply_to_qubits(operators, qubits,
+                          _as_vector(state_tensor, num_qubits))
+    return _as_tensor(out, num_qubits)
+
+
+def swap_tensor(state_tensor: torch.Tensor, qubit_pair: Tuple[int, int],
+                num_qubits: int) -> torch.Tensor:
+    """Two qubit dims exchanged, as a view (operations.py:520-537)."""
+    if qubit_pair[0] == qubit_pair[1]:
+        return state_tensor
+    q1, q2 = get_qubit_indices(index=qubit_pair, state_tensor=state_tensor,
+                               num_qubits=num_qubits)
+    return state_tensor.transpose(q1, q2)
+
+
+def roll_qubits_tensor(state_tensor: torch.Tensor, num_qubits: int,
+                       num_steps: int = 1) -> torch.Tensor:
+    """Cyclic shift of the qubit dims by num_steps, as a view
+    (operations.py:565-597)."""
+    nb = count_batch_dims_tensor(state_tensor, num_qubits)
+    num_steps = num_steps % num_qubits
+    if num_steps == 0:
+        return state_tensor
+    ident = list(range(nb, nb + num_qubits))
+    perm = ident[-num_steps:] + ident[:-num_steps]
+    return state_tensor.permute(list(range(nb)) + perm)
+
+
+def permute_qubits_tensor(permutation: Iterable[int],
+                          state_tensor: torch.Tensor, num_qubits: int,
+                          contiguous_output: bool = False) -> torch.Tensor:
+    """Qubit dims permuted (output qubit j = input qubit permutation[j]),
+    batch dims untouched (operations.py:626-654).  A view, as in unitair;
+    with contiguous_output the permuted amplitudes are written by the tiled
+    permutation kernel."""
+    perm = [int(p) for p in permutation]
+    nb = state_tensor.dim() - num_qubits
+    if not contiguous_output:
+        return torch.permute(state_tensor,
+                             tuple(range(nb)) + tuple(p + nb for p in perm))
+    if sorted(perm) != list(range(num_qubits)):
+        raise RuntimeError(f"permute(): {perm} is not a permutation of the "
+                           f"{num_qubits} qubit dims")
+    out = _permute(_as_vector(state_tensor, num_qubits), perm, num_qubits)
+    return _as_tensor(out, num_qubits)

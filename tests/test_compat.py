@@ -27,7 +27,10 @@ _MODULES = {
         "apply_operator", "apply_all_qubits", "apply_phase",
         "act_first_qubits", "act_last_qubit", "apply_to_qubits", "swap",
         "permute_qubits", "roll_qubits", "multi_cz", "multi_controlled_z",
-        "multi_controlled_x"],
+        "multi_controlled_x", "apply_operator_tensor",
+        "act_first_qubits_tensor", "act_last_qubit_tensor",
+        "apply_all_qubits_tensor", "apply_to_qubits_tensor", "swap_tensor",
+        "roll_qubits_tensor", "permute_qubits_tensor"],
     "unitair.simulation.measurement": ["measure"],
     "unitair.states": ["inner_product", "norm_squared", "abs_squared",
                        "diag_expectation_value"],

@@ -166,3 +166,46 @@ def test_measure_offset_view():
     a = ug.measurement.sample(view, 5000, seed=2).cpu().numpy()
     b = ug.measurement.sample(view.clone(), 5000, seed=2).cpu().numpy()
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("dtype", [torch.complex64, torch.complex128])
+def test_tensor_layout_variants(dtype):
+    """The *_tensor functions equal the vector-layout functions (pinned to
+    the reference by the golden vectors) on the same states, viewed in
+    tensor layout, and the contiguous permutation equals the view's copy."""
+    from qcware_unitair_gb300 import gates as Gt
+    from qcware_unitair_gb300.states import to_tensor_layout
+    n, B = 7, 3
+    g = torch.Generator(device=DEV).manual_seed(3)
+    psi = torch.randn(B, 2 ** n, dtype=dtype, device=DEV, generator=g)
+    T = to_tensor_layout(psi)
+    rx = Gt.exp_x(0.3, dtype=dtype).to(DEV)
+    cn = Gt.cnot(dtype=dtype).to(DEV)
+    u3 = torch.linalg.qr(torch.randn(8, 8, dtype=dtype, device=DEV,
+                                     generator=g))[0]
+    eq = (lambda a, b: torch.allclose(a, b, atol=1e-6 if dtype ==
+                                      torch.complex64 else 1e-13, rtol=0))
+    for op, q in ((rx, [4]), (cn, [5, 1]), (u3, [6, 0, 3])):
+        got = ug.simulation.apply_operator_tensor(op, q, T, n)
+        assert got.shape == T.shape
+        assert eq(got, to_tensor_layout(ug.apply_operator(op, q, psi)))
+    got = ug.simulation.act_first_qubits_tensor(cn, T, n)
+    assert eq(got, to_tensor_layout(ug.apply_operator(cn, [0, 1], psi)))
+    got = ug.simulation.apply_all_qubits_tensor(rx, T, n)
+    assert eq(got, to_tensor_layout(ug.apply_all_qubits(rx, psi)))
+    ops = [rx, Gt.exp_z(0.7, dtype=dtype).to(DEV), rx]
+    got = ug.simulation.apply_to_qubits_tensor(ops, [2, 5, 2], T, n)
+    assert eq(got, to_tensor_layout(ug.apply_to_qubits(ops, [2, 5, 2],
+                                                       psi)))
+    # the last tensor dim contracted with the operator
+    got = ug.simulation.act_last_qubit_tensor(rx, T)
+    ref = torch.einsum("ab,...b->...a", rx.to(torch.complex128),
+                       T.to(torch.complex128))
+    assert eq(got.to(torch.complex128), ref)
+    perm = [3, 0, 6, 1, 5, 2, 4]
+    got = ug.simulation.permute_qubits_tensor(perm, T, n,
+                                              contiguous_output=True)
+    assert got.is_contiguous()
+    assert torch.equal(got,
+                       ug.simulation.permute_qubits_tensor(perm, T, n)
+                       .contiguous())

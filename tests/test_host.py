@@ -1,6 +1,7 @@
 """Host-side logic of the drop-in, on CPU: validation order and exception
 types, and the batch-broadcast plan, against what the reference did for
 the same shapes (tests/golden/cases.json, recorded from unitair)."""
+import numpy as np
 import pytest
 import torch
 
@@ -176,3 +177,41 @@ def test_public_names_of_unitair_present():
                        (G, gate_names)):
         missing = [n for n in names if not hasattr(mod, n)]
         assert not missing, (mod.__name__, missing)
+
+
+def test_tensor_layout_permutations_are_views():
+    """swap_tensor, roll_qubits_tensor and permute_qubits_tensor (without
+    contiguous_output) are views, as in unitair (operations.py:520-654):
+    no data moves and the result aliases the input."""
+    n = 4
+    x = torch.arange(3 * 2 ** n, dtype=torch.float32).view(3, *(n * [2]))
+    a = x.numpy()
+    s = sim.swap_tensor(x, (0, 3), n)
+    assert s.data_ptr() == x.data_ptr()
+    assert np.array_equal(s.numpy(), np.swapaxes(a, 1, 4))
+    assert np.array_equal(sim.swap_tensor(x, (1, -1), n).numpy(),
+                          np.swapaxes(a, 2, 4))
+    assert sim.swap_tensor(x, (2, 2), n) is x
+    with pytest.raises(ValueError):
+        sim.swap_tensor(x, (0, n), n)
+    # psi_rolled[a_0, ..., a_{n-1}] = psi[a_k, ..., a_{n-1}, a_0, ..., a_{k-1}]
+    r = sim.roll_qubits_tensor(x, n, 1)
+    assert r.data_ptr() == x.data_ptr()
+    idx = (1, 0, 1, 1)
+    k = 1
+    src = idx[k:] + idx[:k]
+    assert r[(2,) + idx] == x[(2,) + src]
+    assert sim.roll_qubits_tensor(x, n, n) is x
+    p = sim.permute_qubits_tensor([2, 0, 3, 1], x, n)
+    assert p.data_ptr() == x.data_ptr()
+    assert np.array_equal(p.numpy(), np.transpose(a, (0, 3, 1, 4, 2)))
+
+
+def test_tensor_layout_shape_checks():
+    with pytest.raises(S.StateShapeError):
+        sim._as_vector(torch.zeros(4, 3, 2), 2)
+    with pytest.raises(ValueError):
+        sim.act_last_qubit_tensor(torch.zeros(4, 4, dtype=torch.complex64),
+                                  torch.zeros(2, 2, dtype=torch.complex64))
+    with pytest.raises(ValueError):
+        sim._check_gate_qubits(torch.zeros(2, 2), 2)
