@@ -6,7 +6,7 @@ same torch tensors (vector layout, qubit 0 = most significant index bit,
 unitair's batch broadcasting).  Every operation is a hand-written sm_103a
 CUDA kernel reached through the C ABI in include/gbsv.h; CUDA tensors only.
 """
-from . import gates, states, simulation, initializations  # noqa: F401
+from . import gates, states, simulation, initializations, utils  # noqa: F401
 from .states import (StateLayout, StateShapeError, count_qubits,  # noqa
                      hilbert_space_dim, diag_expectation_value,
                      inner_product, norm_squared, abs_squared)

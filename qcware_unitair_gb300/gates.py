@@ -14,6 +14,7 @@ the hot path.
 """
 from __future__ import annotations
 
+import functools
 import math
 from typing import Dict, Iterable, Optional, Union
 
@@ -150,3 +151,82 @@ def fuse_single_qubit_operators(
     for q, op in zip(qubits, operators):
         fused[q] = torch.matmul(op, fused[q]) if q in fused else op
     return fused
+
+
+# ------------------------------------------- gate construction helpers ---
+# unitair builds its gates with two decorators and a nested stack
+# (gates/gate_construction.py:6-94).  Same behaviour here, without the
+# third-party ``decorator`` package: both work bare or with keywords.
+def nested_stack(params, roll: bool = False) -> torch.Tensor:
+    """A tensor from a nested list of equally sized tensors: [[a, b],
+    [c, d]] with a..d of size (5,) -> (2, 2, 5), or (5, 2, 2) with roll
+    (the tensors' own dims moved to the front as batch dims)."""
+    # every nesting level drops a leading size-1 dim, as unitair's does
+    if isinstance(params[0], torch.Tensor):
+        out = torch.stack(list(params))
+    else:
+        out = torch.stack([nested_stack(x) for x in params])
+    out = out.squeeze(0)
+    if not roll:
+        return out
+    inner = params
+    while not isinstance(inner, torch.Tensor):
+        inner = inner[0]
+    k = inner.dim()
+    d = out.dim()
+    return out.permute(list(range(d - k, d)) + list(range(d - k)))
+
+
+def parameterized_gate(gate_function=None, strictly_complex: bool = False):
+    """Decorator: the gate function receives its parameters as a 1-d tensor
+    (a float or a 0-d tensor becomes one entry, squeezed away again in the
+    result) and returns a tensor or a nested list of tensors, stacked with
+    the parameter dims in front.  As in unitair, only the parameters reach
+    the gate function."""
+    if gate_function is None:
+        return functools.partial(parameterized_gate,
+                                 strictly_complex=strictly_complex)
+
+    @functools.wraps(gate_function)
+    def build(params, *args, **kwargs):
+        squeeze = False
+        if not isinstance(params, torch.Tensor):
+            params = torch.tensor([float(params)], device=torch.device("cpu"))
+            squeeze = True
+        elif params.dim() == 0:
+            params = params.unsqueeze(0)
+            squeeze = True
+        gate = gate_function(params)
+        if not isinstance(gate, torch.Tensor):
+            gate = nested_stack(gate, roll=True)
+        if squeeze:
+            gate = gate.squeeze(0)
+        if strictly_complex and not torch.is_complex(gate):
+            raise TypeError(
+                "This parameterized gate is required to be complex but the\n"
+                f"gate ended up having dtype {gate.dtype}. Check the\n"
+                "construction of the gate decorated with parameterized_gate,"
+                "\nand ensure that it returns a complex Tensor with the given"
+                f"\nparameters (which have dtype {params.dtype}).")
+        return gate
+    return build
+
+
+def constant_gate(gate_function=None, strictly_complex: bool = False):
+    """Decorator: the gate function returns nested lists of numbers; the
+    gate is that tensor on ``device`` (CPU by default) in ``dtype``."""
+    if gate_function is None:
+        return functools.partial(constant_gate,
+                                 strictly_complex=strictly_complex)
+
+    @functools.wraps(gate_function)
+    def build(device=None, dtype=None):
+        gate = torch.tensor(gate_function(),
+                            device=device or torch.device("cpu"))
+        if dtype is not None:
+            gate = gate.to(dtype=dtype)
+        if strictly_complex and not torch.is_complex(gate):
+            raise TypeError("This gate requires a complex dtype, but it ended "
+                            f"up with dtype {gate.dtype}.")
+        return gate
+    return build
