@@ -38,7 +38,8 @@ def _apply(psi, mat, pos, n, cmask=0, cval=0):
 
 def _run_records(prog, psi):
     n, rb = prog.n, prog.rb
-    recs = prog.gate_records.cpu().numpy().view(FG_DTYPE)
+    raw = prog.gate_records.cpu().numpy()  # a placeholder when empty
+    recs = raw[:raw.size - raw.size % FG_DTYPE.itemsize].view(FG_DTYPE)
     lays = (prog.layout_records.cpu().numpy().view(LAYOUT_DTYPE)
             if prog.num_layouts else None)
     pool = prog.pool.cpu().numpy().astype(np.complex128)
@@ -201,3 +202,42 @@ def test_executor_detects_a_wrong_record(oracle):
     ref = oracle.run_circuit([(g.matrix(), g.qubits) for g in circ_gates],
                              psi0)
     assert np.abs(got - ref).max() > 1e-3
+
+
+def test_planners_on_random_circuits_and_tiles(oracle):
+    """Property search over circuits and tile parameters (both planners,
+    layouts on and off): the records always reproduce the circuit."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+    from qcware_unitair_gb300 import _lib
+    L = _lib.load()
+
+    @hyp.settings(max_examples=60, deadline=None)
+    @hyp.given(n=st.integers(2, 9), seed=st.integers(0, 10 ** 6),
+               num=st.integers(1, 60), native=st.booleans(),
+               layouts=st.booleans(), c128=st.booleans(),
+               general=st.booleans(), data=st.data())
+    def run(n, seed, num, native, layouts, c128, general, data):
+        dtype = torch.complex128 if c128 else torch.complex64
+        code = _lib.C128 if c128 else _lib.C64
+        m = data.draw(st.integers(min(n, 2), min(n, int(
+            L.gbsv_fused_max_tile_qubits(code)))))
+        cmin = data.draw(st.integers(0 if c128 else 1, m))
+        if general:
+            circ, listing = _general_circuit(n, num, seed)
+        else:
+            gates = random_circuit(n, num, seed=seed)
+            circ = Circuit.from_gates(n, gates)
+            listing = [(g.matrix(), g.qubits) for g in gates]
+        prog = circ.compile(dtype, "cpu", tile_qubits=m, min_contiguous=cmin,
+                            layouts=layouts, native=native)
+        rng = np.random.default_rng(seed)
+        psi0 = rng.normal(size=(1, 2 ** n)) + 1j * rng.normal(
+            size=(1, 2 ** n))
+        psi0 /= np.linalg.norm(psi0)
+        got = _run_records(prog, psi0.copy())
+        ref = oracle.run_circuit(listing, psi0)
+        tol = 1e-4 if dtype == torch.complex64 else 1e-11
+        assert np.abs(got - ref).max() <= tol
+
+    run()
