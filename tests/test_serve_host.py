@@ -49,3 +49,26 @@ def test_split_into_whole_state_blocks():
     assert small.split(160e9) == [small]
     huge = Request(5, 0.0, 33, 8, [], want_grad=True)  # one block > budget
     assert huge.split(160e9) == [huge]
+
+
+def test_merge_parts_joins_in_state_order():
+    """The outputs of a split request's parts are joined by state offset,
+    whatever order the parts finished in."""
+    from qcware_unitair_gb300.serve import Result, _merge_parts
+    def part(off, k, admitted, done, grads=True):
+        return (off, Result(7, np.arange(off, off + k, dtype=float),
+                            -np.arange(off, off + k, dtype=float),
+                            np.full((k, 3), off, dtype=float) if grads
+                            else None, 1.0, admitted, done))
+    merged = _merge_parts([part(16, 4, 2.5, 3.0), part(0, 8, 1.5, 4.0),
+                           part(8, 8, 2.0, 3.5)])
+    assert merged.rid == 7
+    assert merged.norms.tolist() == list(range(20))
+    assert merged.z0.tolist() == [-float(i) for i in range(20)]
+    assert merged.grads.shape == (20, 3)
+    assert merged.grads[:, 0].tolist() == [0.0] * 8 + [8.0] * 8 + [16.0] * 4
+    assert (merged.arrival, merged.admitted, merged.done) == (1.0, 1.5, 4.0)
+    assert merged.final is None
+    plain = _merge_parts([part(0, 8, 1.0, 2.0, False),
+                          part(8, 2, 1.0, 2.0, False)])
+    assert plain.grads is None and plain.norms.shape == (10,)
