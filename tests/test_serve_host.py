@@ -1,5 +1,6 @@
 """Serving host logic on CPU: the synthetic trace and its accounting."""
 import numpy as np
+import pytest
 
 from qcware_unitair_gb300.serve import Request, make_trace
 
@@ -72,3 +73,33 @@ def test_merge_parts_joins_in_state_order():
     plain = _merge_parts([part(0, 8, 1.0, 2.0, False),
                           part(8, 2, 1.0, 2.0, False)])
     assert plain.grads is None and plain.norms.shape == (10,)
+
+
+def test_split_properties():
+    """Any request and budget: the parts cover the states once, in order,
+    in whole 8-state blocks, and each fits the budget whenever one block
+    does."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+    from qcware_unitair_gb300.serve import STATE_BLOCK
+
+    @hyp.settings(max_examples=300, deadline=None)
+    @hyp.given(n=st.integers(1, 30), states=st.integers(1, 200),
+               grad=st.booleans(), budget=st.floats(1e3, 3e11))
+    def check(n, states, grad, budget):
+        req = Request(1, 0.5, n, states, [], want_grad=grad, seed=3)
+        parts = req.split(budget)
+        assert sum(p.num_states for p in parts) == states
+        k = 0
+        for p in parts:
+            assert p.state_offset == k
+            k += p.num_states
+        if len(parts) > 1:
+            assert all(p.state_offset % STATE_BLOCK == 0 for p in parts)
+            assert all(p.footprint <= budget for p in parts)
+        else:
+            assert parts[0] is req
+            assert (req.footprint <= budget or
+                    STATE_BLOCK * req.bytes_per_state > budget)
+
+    check()
