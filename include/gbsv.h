@@ -4,7 +4,7 @@
  * Every entry point takes raw device pointers, plain sizes and a
  * cudaStream_t passed as void*, returns an int status (GBSV_OK == 0) and
  * never allocates or frees caller memory.  Nothing here names a torch type;
- * a ctypes / cffi binding (see INTEGRATION.md) is all a Python caller needs.
+ * a ctypes / cffi binding is all a Python caller needs.
  *
  * Layout contract (identical to unitair's "vector layout"):
  *   - a state is 2^n complex amplitudes, contiguous, interleaved (re, im);
@@ -395,11 +395,14 @@ int gbsv_norm_squared(const void* state, int dtype, int64_t num_rows,
  * device.  Same inputs and outputs as gbsv_norm_squared; the FP64 partial
  * sums live in a fixed 64 KiB device array inside the library (held on every
  * GPU that loads it until exit) instead of caller scratch, and a request
- * whose partials do not fit is rejected with GBSV_ERR_UNSUPPORTED.  The
- * first call on a device looks up that array's device address, so make it
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race.  Calls no cudaMalloc/cudaFree.  No counterpart in the
- * reference (unitair allocates through torch). */
+ * whose partials do not fit is rejected with GBSV_ERR_UNSUPPORTED.  Each
+ * call looks up that array's device address in the current context (no
+ * allocation, no synchronization); under lazy module loading the first call
+ * on a device also loads the library's device code, which can synchronize,
+ * so make one warm-up call outside a latency-critical loop and before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race.  Calls no cudaMalloc/cudaFree.  No counterpart in the reference
+ * (unitair allocates through torch). */
 int gbsv_norm_squared_noalloc(const void* state, int dtype, int64_t num_rows,
                               int64_t dim, void* out, int out_dtype,
                               void* stream);

@@ -11,7 +11,6 @@
 // Otherwise every block writes an FP64 partial into caller-provided scratch
 // and a second kernel sums the partials of each row in a fixed order, so the
 // result is deterministic (no atomics).
-#include <mutex>
 #include <type_traits>
 
 #include "common.cuh"
@@ -612,31 +611,21 @@ constexpr size_t NOALLOC_SCRATCH_BYTES = 64 * 1024;
 static __device__ __align__(256) double
     g_noalloc_partials[NOALLOC_SCRATCH_BYTES / sizeof(double)];
 
-constexpr int NOALLOC_MAX_DEVICES = 64;
-static std::mutex g_noalloc_mutex;
-static double* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
-
-// Device address of g_noalloc_partials on the current device, looked up
-// once per device (host code may not use the symbol's host-side name as a
-// device pointer).
+// Device address of g_noalloc_partials in the current device's context.
+// Host code may not use the symbol's host-side name as a device pointer, so
+// the address is looked up on every call: the lookup allocates nothing and
+// does not synchronize, and a cached address would go stale when the
+// context is torn down and recreated (cudaDeviceReset).  Under lazy module
+// loading the first lookup on a device loads this module, which can
+// synchronize; a warm-up call before a latency-critical loop or a stream
+// capture moves that cost out of the loop.
 static int noalloc_scratch(double** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess)
-    return set_error(GBSV_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
-  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
-    return set_error(GBSV_ERR_UNSUPPORTED, "device %d beyond %d", dev,
-                     NOALLOC_MAX_DEVICES);
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_partials);
-    if (e != cudaSuccess || !p)
-      return set_error(GBSV_ERR_CUDA, "cudaGetSymbolAddress: %s",
-                       cudaGetErrorString(e));
-    g_noalloc_ptr[dev] = static_cast<double*>(p);
-  }
-  *out = g_noalloc_ptr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+  if (e != cudaSuccess || !p)
+    return set_error(GBSV_ERR_CUDA, "cudaGetSymbolAddress: %s",
+                     cudaGetErrorString(e));
+  *out = static_cast<double*>(p);
   return GBSV_OK;
 }
 
