@@ -192,6 +192,58 @@ int gbsv_run_programs(int dtype, int num_qubits, int num_ctas,
                       const void* gate_count, const void* gates,
                       const void* pool, void* stream);
 
+/* ---- tensor-core stages (complex64) ------------------------------------ */
+
+/* One block of a tensor-core stage (64 bytes, device memory): a 32x32
+ * matrix on the 5 tile bits that index a thread's registers.  Offsets are
+ * in amplitudes within the swizzled tile (amplitude index bits 1-3 XOR
+ * bits 4-6, 7-9 and 10-12): rspo[k] for register-index bit k, tspo[j] for
+ * thread-index bit j (128 threads).  mat indexes the image array (16 KiB
+ * per block: the integer part Bh of 1024 * B then the residual
+ * 2048 * (1024 * B - Bh), both fp16 in the tensor cores' K-major
+ * no-swizzle layout, B the 64x64 real form of U^T).  Post-diagonals
+ * diags[first_diag .. first_diag + num_diag) run after the block. flags bit
+ * 0: register bit 0 is tile bit 0. */
+typedef struct gbsv_tc_block {
+  int32_t rspo[5];
+  int32_t tspo[7];
+  int32_t mat;
+  int32_t first_diag;
+  int32_t num_diag;
+  int32_t flags;
+} gbsv_tc_block_t;
+
+/* A 1- or 2-qubit diagonal applied after a block (48 bytes): each qubit is
+ * a register bit (0..4), a thread-index bit (5 + j) or -1 - its position
+ * outside the tile; qubit 0 is the MSB of the value index; reg != 0 when a
+ * qubit is a register bit. */
+typedef struct gbsv_tc_diag {
+  int32_t nq;
+  int32_t enc[2];
+  int32_t reg;
+  float d[8];
+} gbsv_tc_diag_t;
+
+/* One fused stage on the tensor cores: 12 tile bits (tile_positions, the
+ * first contiguous_qubits of them the positions 0, 1, ...; the rest any
+ * order), applied block by block with tcgen05.mma (A = the tile's columns
+ * in tensor memory, B = the block image in shared memory), one HBM pass.
+ * complex64 only, num_qubits >= 12, 1..64 blocks, states and images 16-byte
+ * aligned; in place when state_in == state_out.  Generalises the
+ * contraction unitair runs per gate (operations.py:322, torch.einsum over
+ * the gate's qubit axes) to a product of gates applied as one matrix. */
+int gbsv_run_stage_tc(const void* state_in, void* state_out, int dtype,
+                      int num_qubits, int64_t num_states, int64_t in_stride,
+                      int tile_qubits, int contiguous_qubits,
+                      const int32_t* tile_positions, const void* blocks,
+                      int num_blocks, const void* diags, const void* images,
+                      void* stream);
+
+/* Nonzero bits record a bounded wait inside a tensor-core stage that ran out
+ * (1: block image, 2: MMA completion, 4 / 8: draining); clear != 0 resets
+ * it.  Synchronizes the device.  No counterpart in the reference. */
+int gbsv_tc_status(int* status, int clear);
+
 /* ---- permutations, multi-controlled gates, sampling -------------------- */
 
 /* out qubit j <- in qubit perm[j] (perm a HOST array of num_qubits entries;

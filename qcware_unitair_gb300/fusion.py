@@ -151,9 +151,10 @@ class Circuit:
     def compile(self, dtype=torch.complex64, device="cuda", fuse=True,
                 tile_qubits: Optional[int] = None,
                 min_contiguous: Optional[int] = None,
-                layouts: bool = True, native: bool = True) -> "Program":
+                layouts: bool = True, native: bool = True,
+                tensor_cores: Optional[bool] = None) -> "Program":
         return Program(self, dtype, torch.device(device), fuse, tile_qubits,
-                       min_contiguous, layouts, native)
+                       min_contiguous, layouts, native, tensor_cores)
 
     def run(self, state: torch.Tensor, fuse: bool = True,
             inplace: bool = False) -> torch.Tensor:
@@ -489,8 +490,9 @@ class Program:
 
     def __init__(self, circuit: Circuit, dtype, device, fuse=True,
                  tile_qubits=None, min_contiguous=None, layouts=True,
-                 native=True):
+                 native=True, tensor_cores=None):
         self.native = False
+        self.tensor_cores = False
         self.n = n = circuit.num_qubits
         self.dtype = dtype
         self.device = device
@@ -516,6 +518,20 @@ class Program:
                     raise ValueError("per-state gates must share one batch "
                                      "size")
                 self.batch = b
+        # tensor-core stages: complex64, shared matrices, 12-bit tiles
+        tc_ok = (fuse and dtype == torch.complex64 and n >= 12
+                 and self.batch is None and tile_qubits in (None, 12))
+        if tensor_cores is None:
+            tensor_cores = tc_ok and layouts
+        if tensor_cores:
+            if not tc_ok:
+                raise ValueError("tensor-core stages need complex64, at "
+                                 "least 12 qubits, shared gate matrices and "
+                                 "12 tile qubits")
+            from . import tcplan
+            self.m = tcplan.TC_M
+            self._build_tc(tcplan.plan_tc(circuit.gates, n, self.c_min))
+            return
         nat = None
         if native:
             nat = native_plan(circuit.gates, n, self.m, self.c_min,
@@ -592,6 +608,41 @@ class Program:
         self.native = True
 
     # -- packing ---------------------------------------------------------
+    def _plain_op(self, g):
+        mat = g.matrix.to(dtype=self.dtype).contiguous()
+        if self.device.type == "cuda" and not mat.is_cuda:
+            mat = mat.pin_memory()
+        return ("plain", mat.to(self.device, non_blocking=True), g.qubits)
+
+    def _build_tc(self, raw):
+        """Tensor-core stages (tcplan) and single-gate launches."""
+        from . import tcplan
+        dev = self.device
+        blocks, diags, images = [], [], []
+        self.ops = []
+        for kind, item in raw:
+            if kind == "plain":
+                self.ops.append(self._plain_op(item))
+                continue
+            first = len(blocks)
+            c, order = tcplan.encode_stage(item, self.n, blocks, diags,
+                                           images)
+            positions = (ctypes.c_int32 * tcplan.TC_M)(*order)
+            self.ops.append(("tc", c, positions, first, len(blocks) - first))
+        self.tc_blocks = _to_device(
+            np.stack(blocks).view(np.uint8) if blocks else None, dev)
+        self.tc_diags = _to_device(
+            np.stack(diags).view(np.uint8) if diags else None, dev)
+        self.tc_images = _to_device(
+            np.concatenate(images).view(np.uint8) if images else None, dev)
+        self.tc_records = (blocks, diags, images)  # host copies (tests)
+        self.gate_records = self.layout_records = _to_device(None, dev)
+        self.num_layouts = 0
+        self.pool = torch.zeros(1, dtype=self.dtype, device=dev)
+        self.num_stages = sum(1 for o in self.ops if o[0] != "plain")
+        self.num_plain = sum(1 for o in self.ops if o[0] == "plain")
+        self.tensor_cores = True
+
     def _build(self, raw):
         n, dev, dt = self.n, self.device, self.dtype
         records = []
@@ -720,6 +771,15 @@ class Program:
                                       positions, gp + first * 48, count,
                                       pool, stream)
                 _lib.check(rc, "run_stage")
+            elif op[0] == "tc":
+                _, c, positions, first, count = op
+                rc = L.gbsv_run_stage_tc(
+                    cur.data_ptr(), out.data_ptr(), self.code, self.n, B, N,
+                    self.m, c, positions,
+                    self.tc_blocks.data_ptr() + first * 64, count,
+                    self.tc_diags.data_ptr(), self.tc_images.data_ptr(),
+                    stream)
+                _lib.check(rc, "run_stage_tc")
             elif op[0] == "layouts":
                 _, c, positions, first, count = op
                 rc = L.gbsv_run_stage_layouts(

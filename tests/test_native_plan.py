@@ -9,6 +9,7 @@ from qcware_unitair_gb300.fusion import Circuit
 
 
 def _cmp(circ, dtype, **kw):
+    kw.setdefault("tensor_cores", False)  # the register-stage planners
     a = circ.compile(dtype, "cpu", native=True, **kw)
     b = circ.compile(dtype, "cpu", native=False, **kw)
     assert a.native and not b.native
