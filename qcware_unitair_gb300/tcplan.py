@@ -271,13 +271,14 @@ def encode_stage(plan: TcStagePlan, n: int, blocks_out: list,
         U = np.eye(32, dtype=np.complex128)
         for it in blk.gates:
             g = it.gate
-            mat = g.matrix.detach().cpu().numpy().astype(np.complex128)
+            mat = g.matrix.detach().cpu().resolve_conj().numpy().astype(
+                np.complex128)
             kb = [kpos[n - 1 - q] for q in g.qubits]
             U = _embed(mat, kb) @ U
         first_diag = len(diags_out)
         for it in blk.post:
             g = it.gate
-            vals = np.diagonal(g.matrix.detach().cpu().numpy()).astype(
+            vals = np.diagonal(g.matrix.detach().cpu().resolve_conj().numpy()).astype(
                 np.complex64)
             rec = np.zeros((), dtype=DIAG_DTYPE)
             rec["nq"] = len(g.qubits)
