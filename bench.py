@@ -55,6 +55,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the adjoint and serving measurements")
+    p.add_argument("--workload", nargs="+", default=None,
+                   help="run one small profiling workload (see the "
+                        "workloads section) instead of the benchmark")
     return p.parse_args()
 
 
@@ -66,19 +69,12 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """Per-launch DRAM bytes of the dense gate kernel from the committed ncu
-    summary (a `traffic_bytes_per_launch = N` line), or None."""
-    f = REPO / "profiles" / "dense_gate_30q_c64.md"
-    if not f.exists():
-        return None
-    for line in f.read_text().splitlines():
-        if line.strip().startswith("traffic_bytes_per_launch"):
-            try:
-                return float(line.split("=")[1].split()[0])
-            except (IndexError, ValueError):
-                return None
-    return None
+# DRAM bytes (read + write) of one dense_chunk_kernel launch on a 30-qubit
+# complex64 state: ncu dram__bytes_read.sum + dram__bytes_write.sum of a
+# 26-qubit capture, scaled by 16 (traffic is proportional to the state; a
+# 30-qubit capture is beyond the capture-size rule).
+DENSE_GATE_TRAFFIC_30Q = 16_238_000_000
+DENSE_GATE_TRAFFIC_SOURCE = "ncu 26q x16"
 
 
 # ----------------------------------------------------------- distributed --
@@ -672,6 +668,192 @@ def parse_cpulist(txt: str) -> set:
     return cpus
 
 
+# ------------------------------------------------------------ workloads --
+# Small fixed workloads for timing and profiling one kernel at a time
+# (python bench.py --workload NAME [ARGS]); each runs twice (a warm-up, then
+# a CUDA-event-timed run) and prints one line, so under a profiler skip the
+# first run's launches.
+#   stage N [GATES]      canonical random circuit (numpy seed 0), complex64,
+#                        fused (tensor-core stages), in place from |0...0>
+#   stage_reg N [GATES]  the same on the register-blocked stages
+#   gates N KIND K       one register stage: 8 Hadamards on spread tile bits
+#                        plus K copies of KIND (H, X, RX, RZout = RZ on a bit
+#                        that is never a register bit)
+#   adjoint B            20-qubit, 12-layer ansatz forward + adjoint backward
+#   serve NUM            the serving trace (150/s, 10-22 qubits) on the server
+#                        after a 16-request warm-up, with host time per path
+#   kinds N              one plain complex128 gate of each kind, 10 launches
+def _wl_timed(fn):
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def wl_stage(n: int = 26, gates: int = 200, tensor_cores=None) -> float:
+    import torch
+    from qcware_unitair_gb300.circuits import random_circuit, zero_state
+    from qcware_unitair_gb300.fusion import Circuit
+    dev = torch.device("cuda")
+    prog = Circuit.from_gates(n, random_circuit(n, gates, seed=0)).compile(
+        torch.complex64, dev, tensor_cores=tensor_cores)
+    psi = zero_state(n, (), torch.complex64, dev)
+    ms = _wl_timed(lambda: prog.run(psi, inplace=True))
+    print(f"stage n={n} gates={gates} tensor_cores={prog.tensor_cores} "
+          f"passes={prog.num_passes} {ms:.3f} ms")
+    return ms
+
+
+def wl_gates(n: int = 24, kind: str = "H", k: int = 64) -> float:
+    import torch
+    from qcware_unitair_gb300.circuits import gate_matrix
+    from qcware_unitair_gb300.fusion import Circuit
+    dev = torch.device("cuda")
+
+    def q(bit):
+        return n - 1 - bit
+
+    c = Circuit(n)
+    for b in (6, 8, 10, 12, 14, 16, 18, 20):
+        c.h(q(b))
+    for i in range(k):
+        if kind == "H":
+            c.h(q(0))
+        elif kind == "X":
+            c.x(q(0))
+        elif kind == "RX":
+            c.append(gate_matrix("RX", 0.3 + i), [q(0)], "dense")
+        elif kind == "RZout":
+            c.append(gate_matrix("RZ", 0.3 + i), [q(5)], "diag")
+        else:
+            raise ValueError(f"unknown gate kind {kind}")
+    prog = c.compile(torch.complex64, dev, tile_qubits=12,
+                     tensor_cores=False)
+    psi = torch.randn(2 ** n, dtype=torch.complex64, device=dev)
+    ms = _wl_timed(lambda: prog.run(psi, inplace=True))
+    print(f"gates n={n} kind={kind} k={k} passes={prog.num_passes} "
+          f"{ms:.3f} ms")
+    return ms
+
+
+def wl_adjoint(batch: int = 16, n: int = 20, layers: int = 12) -> float:
+    import torch
+    from qcware_unitair_gb300.adjoint import PauliSum, expectation, hardware_efficient_ansatz
+    dev = torch.device("cuda")
+    pc = hardware_efficient_ansatz(n, layers)
+    H = PauliSum(n)
+    for i in range(n):
+        H.z(i)
+    for i in range(n - 1):
+        H.xx(i, i + 1, coeff=0.5)
+    g = torch.Generator(device=dev)
+    g.manual_seed(0)
+    params = torch.randn(batch, pc.num_params, generator=g, device=dev)
+
+    def step():
+        p = params.clone().requires_grad_()
+        expectation(pc, p, H).mean().backward()
+        return p.grad
+
+    ms = _wl_timed(step)
+    print(f"adjoint n={n} layers={layers} batch={batch} {ms:.3f} ms")
+    return ms
+
+
+def wl_serve(num: int = 300) -> float:
+    import torch
+    import collections
+    import time
+    from qcware_unitair_gb300 import serve as S
+    dev = torch.device("cuda")
+    spent = collections.defaultdict(float)
+
+    def timed(obj, name, key):
+        f = getattr(obj, name)
+
+        def w(*a, **k):
+            t = time.perf_counter()
+            try:
+                return f(*a, **k)
+            finally:
+                spent[key] += time.perf_counter() - t
+        setattr(obj, name, w)
+        return f
+
+    warm = S.make_trace(16, rate=1000.0, seed=99, qubits=(10, 22),
+                        depth=(20, 100))
+    S.Server(dev).serve(warm)
+    saved = [(S.Server, "_launch_small",
+              timed(S.Server, "_launch_small", "small launches")),
+             (S.Server, "_launch_large",
+              timed(S.Server, "_launch_large", "large launches")),
+             (S, "_run_grad", timed(S, "_run_grad", "gradient requests"))]
+    try:
+        trace = S.make_trace(num, rate=150.0, seed=0, qubits=(10, 22))
+        res = S.summarize(S.Server(dev).serve(trace))
+    finally:
+        for obj, name, f in saved:
+            setattr(obj, name, f)
+    print(f"serve {res}; host seconds: "
+          + ", ".join(f"{k} {v:.3f}" for k, v in spent.items()))
+    return res["circuits_per_s"]
+
+
+def wl_kinds(n: int = 28) -> None:
+    import torch
+    import qcware_unitair_gb300 as ug
+    from qcware_unitair_gb300.circuits import gate_matrix
+    dev = torch.device("cuda")
+    psi = torch.randn(2 ** n, dtype=torch.complex128, device=dev)
+    psi /= psi.abs().pow(2).sum().sqrt()
+    cases = [("X", [5]), ("H", [5]), ("RY", [5]), ("RX", [5]), ("RZ", [5]),
+             ("T", [5]), ("Z", [5]), ("Y", [5]), ("CNOT", [3, 20]),
+             ("CZ", [3, 20]), ("SWAP", [3, 20]), ("X", [n - 1]),
+             ("RX", [n - 1]), ("CNOT", [n - 2, n - 1])]
+    for name, q in cases:
+        theta = 0.7 if name.startswith("R") else None
+        m = torch.from_numpy(gate_matrix(name, theta)).to(dev)
+        for _ in range(2):
+            ug.apply_operator_(m, q, psi)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            ug.apply_operator_(m, q, psi)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 10
+        print(f"kinds n={n} {name} {q}: {ms:.3f} ms "
+              f"{2 * 16 * 2 ** n / ms / 1e6:.0f} GB/s")
+
+def run_workload(argv):
+    import torch  # noqa: F401  (CUDA initialised before the workload)
+    what, args = argv[0], argv[1:]
+    if what == "stage":
+        wl_stage(*(int(a) for a in args))
+    elif what == "stage_reg":
+        wl_stage(*(int(a) for a in args), tensor_cores=False)
+    elif what == "gates":
+        wl_gates(int(args[0]) if args else 24,
+                 args[1] if len(args) > 1 else "H",
+                 int(args[2]) if len(args) > 2 else 64)
+    elif what == "adjoint":
+        wl_adjoint(*(int(a) for a in args))
+    elif what == "serve":
+        wl_serve(*(int(a) for a in args))
+    elif what == "kinds":
+        wl_kinds(*(int(a) for a in args))
+    else:
+        raise SystemExit(f"unknown workload {what}")
+
+
 # -------------------------------------------------------------- GPU arm ---
 def run_gpu(args, ws, rank, local):
     import numpy as np
@@ -696,26 +878,23 @@ def run_gpu(args, ws, rank, local):
     psi = torch.zeros(N, dtype=torch.complex64, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    def step(record=None):
+    def reset():
         psi.zero_()
         psi[0] = 1
-        for g, m in zip(gates, mats):
-            if record is not None:
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                ug.apply_operator_(m, g.qubits, psi)
-                e1.record(stream)
-                record.append((e0, e1))
-            else:
-                ug.apply_operator_(m, g.qubits, psi)
 
+    def step():
+        for g, m in zip(gates, mats):
+            ug.apply_operator_(m, g.qubits, psi)
+
+    reset()
     for _ in range(args.warmup):
         step()
+    # Timed: exactly K applications of the circuit, back to back, starting
+    # from |0...0> (reset before the region); nothing else is launched.
+    reset()
     torch.cuda.synchronize()
     barrier()
     torch.cuda.synchronize()
-    events = []
     l0 = _lib.launch_count()
     gc.collect()
     gc.disable()  # no collector pauses inside the timed host loop
@@ -724,7 +903,7 @@ def run_gpu(args, ws, rank, local):
         t1 = torch.cuda.Event(enable_timing=True)
         t0.record(stream)
         for _ in range(args.steps):
-            step(events)
+            step()
         t1.record(stream)
         torch.cuda.synchronize()
     barrier()
@@ -732,44 +911,68 @@ def run_gpu(args, ws, rank, local):
     launches = _lib.launch_count() - l0
     ms = t0.elapsed_time(t1)
     ms = max_over_ranks(ms, dev)
-    per_launch_ms = [a.elapsed_time(b) for a, b in events]
-    # psi.zero_ / psi[0] = 1 are torch fills between circuits: not our kernels
-    gate_ms = statistics.mean(per_launch_ms)
     total_bytes = bytes_per_gate * G * args.steps * ws
     value = total_bytes / (ms / 1e3) / 1e9
 
-    # ---- fused-stage path on the same circuit --------------------------
-    from qcware_unitair_gb300.fusion import Circuit
-    circ = Circuit.from_gates(n, gates)
-    prog = circ.compile(torch.complex64, dev)
-    fused_events = []
-
-    def fused_step(record=None):
-        psi.zero_()
-        psi[0] = 1
-        if record is None:
-            prog.run(psi, inplace=True)
-            return
+    # per-launch durations of the dense gate kernel (roofline), in one more
+    # untimed application of the circuit with events around every launch
+    per_launch_ms = []
+    reset()
+    for g, m in zip(gates, mats):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        prog.run(psi, inplace=True)
+        ug.apply_operator_(m, g.qubits, psi)
         e1.record(stream)
-        record.append((e0, e1))
+        per_launch_ms.append((e0, e1))
+    torch.cuda.synchronize()
+    per_launch_ms = [a.elapsed_time(b) for a, b in per_launch_ms]
+    gate_ms = statistics.mean(per_launch_ms)
 
-    for _ in range(args.warmup):
-        fused_step()
-    torch.cuda.synchronize()
-    barrier()
-    l1 = _lib.launch_count()
-    for _ in range(args.steps):
-        fused_step(fused_events)
-    torch.cuda.synchronize()
-    fused_launches = _lib.launch_count() - l1
-    fused_ms = statistics.mean(a.elapsed_time(b) for a, b in fused_events)
-    fused_ms = max_over_ranks(fused_ms, dev)
-    fused_norm = float(torch.linalg.vector_norm(psi.to(torch.complex128)))
+    # ---- fused paths on the same circuit ------------------------------
+    from qcware_unitair_gb300.fusion import Circuit
+    circ = Circuit.from_gates(n, gates)
+
+    def fused_run(prog):
+        """K timed applications (after W warm-ups) from |0...0>; mean ms per
+        circuit, per-stage launch durations of one more run, the norm."""
+        reset()
+        for _ in range(args.warmup):
+            prog.run(psi, inplace=True)
+        reset()
+        torch.cuda.synchronize()
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        lc = _lib.launch_count()
+        e0.record(stream)
+        for _ in range(args.steps):
+            prog.run(psi, inplace=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        nl = (_lib.launch_count() - lc) // max(1, args.steps)
+        f_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dev)
+        norm = float(torch.linalg.vector_norm(psi.to(torch.complex128)))
+        # per-stage durations (one more run, events around each launch)
+        reset()
+        evs = []
+        for op in prog.ops:
+            a = torch.cuda.Event(enable_timing=True)
+            z = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            prog.run_op(op, psi)
+            z.record(stream)
+            evs.append((op[0], a, z))
+        torch.cuda.synchronize()
+        stage_ms = [a.elapsed_time(z) for k, a, z in evs if k != "plain"]
+        return f_ms, nl, norm, stage_ms
+
+    prog = circ.compile(torch.complex64, dev)
+    fused_ms, fused_launches, fused_norm, tc_stage_ms = fused_run(prog)
     stage_ms = fused_ms / prog.num_passes
+    prog_reg = circ.compile(torch.complex64, dev, tensor_cores=False)
+    reg_ms, _, reg_norm, _ = fused_run(prog_reg)
+    del prog_reg
 
     # ---- e2e through the public functional API, host buffers -----------
     # pinned buffers are placed from the GPU's local CPUs: pages pinned on
@@ -850,7 +1053,6 @@ def run_gpu(args, ws, rank, local):
 
     peak, peak_kind = peaks()
     achieved = bytes_per_gate / (gate_ms / 1e3) / 1e9
-    traffic = profile_traffic()
     result = {
         "metric": METRIC, "value": round(value, 1), "unit": "GB/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -870,7 +1072,8 @@ def run_gpu(args, ws, rank, local):
                      "frac": round(achieved / peak, 4),
                      "peak_source": peak_kind,
                      "kernel": "dense_chunk_kernel (1- and 2-qubit gates)",
-                     "traffic": traffic,
+                     "traffic": DENSE_GATE_TRAFFIC_30Q,
+                     "traffic_source": DENSE_GATE_TRAFFIC_SOURCE,
                      "algorithmic_bytes_per_launch": bytes_per_gate,
                      "launch_ms_mean": round(gate_ms, 4),
                      "launch_ms_p50": round(statistics.median(per_launch_ms),
@@ -882,9 +1085,12 @@ def run_gpu(args, ws, rank, local):
                 "step_parts": e2e_parts,
                 "final_norm_drift": drift},
         "fused": {
+            "engine": "tensor-core stages (tcgen05, 32x32 blocks)"
+                      if prog.tensor_cores else "register stages",
             "ms_per_step": round(fused_ms, 3), "passes": prog.num_passes,
             "gates_per_pass": round(G / prog.num_passes, 2),
             "pass_reduction": round(G / prog.num_passes, 2),
+            "blocks": sum(o[4] for o in prog.ops if o[0] == "tc"),
             "speedup_vs_plain": round((ms / args.steps) / fused_ms, 3),
             "tile_qubits": prog.m,
             "hbm_GBs": round(bytes_per_gate * prog.num_passes /
@@ -894,8 +1100,24 @@ def run_gpu(args, ws, rank, local):
             "gate_equivalent_GBs": round(bytes_per_gate * G /
                                          (fused_ms / 1e3) / 1e9, 1),
             "stage_ms_mean": round(stage_ms, 4),
-            "launches_per_step": fused_launches // max(1, args.steps),
-            "final_norm": fused_norm},
+            "stage_launch_ms_mean": round(statistics.mean(tc_stage_ms), 4)
+                                    if tc_stage_ms else None,
+            "launches_per_step": fused_launches,
+            "final_norm": fused_norm,
+            "register_stages_ms": round(reg_ms, 3),
+            "speedup_vs_register_stages": round(reg_ms / fused_ms, 3),
+            "register_stages_final_norm": reg_norm},
+        "roofline_fused": {
+            "bound": "hbm", "kernel": "tc_stage_kernel" if prog.tensor_cores
+            else "fused_reg_kernel",
+            "achieved": round(bytes_per_gate / (statistics.mean(tc_stage_ms)
+                                                / 1e3) / 1e9, 1)
+                        if tc_stage_ms else None,
+            "peak": peak, "unit": "GB/s",
+            "frac": round(bytes_per_gate / (statistics.mean(tc_stage_ms)
+                                            / 1e3) / 1e9 / peak, 4)
+                    if tc_stage_ms else None,
+            "algorithmic_bytes_per_launch": bytes_per_gate},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
     }
@@ -961,6 +1183,9 @@ def run_reference(args, ws, rank):
 
 def main():
     args = parse()
+    if args.workload:
+        run_workload(args.workload)
+        return
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, ws, rank)

@@ -758,47 +758,57 @@ class Program:
         stream = _core.stream_of(state.device)
         N = 2 ** self.n
         cur = src
-        gp = self.gate_records.data_ptr()
-        lp = self.layout_records.data_ptr()
-        pool = self.pool.data_ptr()
         if not self.ops and cur is not out:
             out.copy_(cur)
         for op in self.ops:
-            if op[0] == "stage":
-                _, c, positions, first, count = op
-                rc = L.gbsv_run_stage(cur.data_ptr(), out.data_ptr(),
-                                      self.code, self.n, B, N, self.m, c,
-                                      positions, gp + first * 48, count,
-                                      pool, stream)
-                _lib.check(rc, "run_stage")
-            elif op[0] == "tc":
-                _, c, positions, first, count = op
-                rc = L.gbsv_run_stage_tc(
-                    cur.data_ptr(), out.data_ptr(), self.code, self.n, B, N,
-                    self.m, c, positions,
-                    self.tc_blocks.data_ptr() + first * 64, count,
-                    self.tc_diags.data_ptr(), self.tc_images.data_ptr(),
-                    stream)
-                _lib.check(rc, "run_stage_tc")
-            elif op[0] == "layouts":
-                _, c, positions, first, count = op
-                rc = L.gbsv_run_stage_layouts(
-                    cur.data_ptr(), out.data_ptr(), self.code, self.n, B, N,
-                    self.m, c, positions, gp, lp + first * 32, count, pool,
-                    stream)
-                _lib.check(rc, "run_stage_layouts")
-            else:
-                _, mat, qubits = op
-                op_stride = 0 if mat.dim() == 2 else mat.shape[-1] ** 2
-                wide = (cur.data_ptr() == out.data_ptr() and len(qubits) >
-                        _core.max_inplace_qubits(self.dtype))
-                dst = torch.empty_like(out) if wide else out
-                rc = L.gbsv_apply_operator(
-                    cur.data_ptr(), dst.data_ptr(), self.code, self.n, B, N,
-                    mat.data_ptr(), op_stride, _lib.qubit_array(qubits),
-                    len(qubits), stream)
-                _lib.check(rc, "apply_operator")
-                if wide:
-                    out.copy_(dst)
+            self._run_op(op, cur, out, B, N, L, stream)
             cur = out
         return out
+
+    def run_op(self, op, state: torch.Tensor) -> None:
+        """One pass of the program (an entry of ``ops``), in place on a
+        contiguous state: for timing the stages one at a time."""
+        B = state.numel() >> self.n
+        self._run_op(op, state, state, B, 2 ** self.n, _lib.load(),
+                     _core.stream_of(state.device))
+
+    def _run_op(self, op, cur, out, B, N, L, stream):
+        gp = self.gate_records.data_ptr()
+        lp = self.layout_records.data_ptr()
+        pool = self.pool.data_ptr()
+        if op[0] == "stage":
+            _, c, positions, first, count = op
+            rc = L.gbsv_run_stage(cur.data_ptr(), out.data_ptr(),
+                                  self.code, self.n, B, N, self.m, c,
+                                  positions, gp + first * 48, count,
+                                  pool, stream)
+            _lib.check(rc, "run_stage")
+        elif op[0] == "tc":
+            _, c, positions, first, count = op
+            rc = L.gbsv_run_stage_tc(
+                cur.data_ptr(), out.data_ptr(), self.code, self.n, B, N,
+                self.m, c, positions,
+                self.tc_blocks.data_ptr() + first * 64, count,
+                self.tc_diags.data_ptr(), self.tc_images.data_ptr(),
+                stream)
+            _lib.check(rc, "run_stage_tc")
+        elif op[0] == "layouts":
+            _, c, positions, first, count = op
+            rc = L.gbsv_run_stage_layouts(
+                cur.data_ptr(), out.data_ptr(), self.code, self.n, B, N,
+                self.m, c, positions, gp, lp + first * 32, count, pool,
+                stream)
+            _lib.check(rc, "run_stage_layouts")
+        else:
+            _, mat, qubits = op
+            op_stride = 0 if mat.dim() == 2 else mat.shape[-1] ** 2
+            wide = (cur.data_ptr() == out.data_ptr() and len(qubits) >
+                    _core.max_inplace_qubits(self.dtype))
+            dst = torch.empty_like(out) if wide else out
+            rc = L.gbsv_apply_operator(
+                cur.data_ptr(), dst.data_ptr(), self.code, self.n, B, N,
+                mat.data_ptr(), op_stride, _lib.qubit_array(qubits),
+                len(qubits), stream)
+            _lib.check(rc, "apply_operator")
+            if wide:
+                out.copy_(dst)
