@@ -199,18 +199,26 @@ int gbsv_run_programs(int dtype, int num_qubits, int num_ctas,
  * in amplitudes within the swizzled tile (amplitude index bits 1-3 XOR
  * bits 4-6, 7-9 and 10-12): rspo[k] for register-index bit k, tspo[j] for
  * thread-index bit j (128 threads).  mat indexes the image array (16 KiB
- * per block: the integer part Bh of 1024 * B then the residual
- * 2048 * (1024 * B - Bh), both fp16 in the tensor cores' K-major
- * no-swizzle layout, B the 64x64 real form of U^T).  Post-diagonals
- * diags[first_diag .. first_diag + num_diag) run after the block. flags bit
- * 0: register bit 0 is tile bit 0. */
+ * per block: B the 64x64 real form of U^T, Bh = rint(1024 * B) and
+ * Bl = 1024 * B - Bh, stored as the fp16 K = 128 x N = 64 operand
+ * [Bl; Bh] in the tensor cores' K-major no-swizzle layout with 8-row
+ * groups 2048 bytes apart).  After the block, amplitudes are scaled by
+ * a per-thread factor factors[fac + p * 128 + thread] (fac >= 0; p = the
+ * state's bits at positions opos[0 .. nout-1], bit k of p from opos[k]) --
+ * the diagonal gates that commute with the block, folded on the host -- and
+ * by the post-diagonals diags[first_diag .. first_diag + num_diag).  flags
+ * bit 0: register bit 0 is tile bit 0. */
 typedef struct gbsv_tc_block {
-  int32_t rspo[5];
-  int32_t tspo[7];
+  int16_t rspo[5];
+  int16_t tspo[7];
   int32_t mat;
   int32_t first_diag;
   int32_t num_diag;
   int32_t flags;
+  int32_t fac;
+  int8_t nout;
+  int8_t opos[7];
+  int32_t pad_[3];
 } gbsv_tc_block_t;
 
 /* A 1- or 2-qubit diagonal applied after a block (48 bytes): each qubit is
@@ -237,7 +245,7 @@ int gbsv_run_stage_tc(const void* state_in, void* state_out, int dtype,
                       int tile_qubits, int contiguous_qubits,
                       const int32_t* tile_positions, const void* blocks,
                       int num_blocks, const void* diags, const void* images,
-                      void* stream);
+                      const void* factors, void* stream);
 
 /* Nonzero bits record a bounded wait inside a tensor-core stage that ran out
  * (1: block image, 2: MMA completion, 4 / 8: draining); clear != 0 resets

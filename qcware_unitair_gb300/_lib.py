@@ -85,7 +85,8 @@ SIGNATURES = {
                                     _P]),
     "gbsv_run_programs": (_I, [_I, _I, _I, _P, _P, _P, _P, _P, _P]),
     "gbsv_run_stage_tc": (_I, [_P, _P, _I, _I, _I64, _I64, _I, _I,
-                               ctypes.POINTER(_I32), _P, _I, _P, _P, _P]),
+                               ctypes.POINTER(_I32), _P, _I, _P, _P, _P,
+                               _P]),
     "gbsv_tc_status": (_I, [ctypes.POINTER(_I), _I]),
     "gbsv_plan": (_I, [_P, _I, _P, _I, _I, _I, _I, _I,
                        ctypes.POINTER(Plan)]),

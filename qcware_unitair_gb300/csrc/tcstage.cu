@@ -21,35 +21,34 @@
 // fp16 split would shrink every amplitude a little per block.  Instead the
 // split makes the dominant product exact:
 //   * each thread scales its 64 reals by a power of two s so the largest is
-//     below 2^10, and splits x*s = hi + lo * 2^-11 with hi an integer
-//     (|hi| <= 1024, exact in fp16) and lo rounded to fp16;
+//     below 2^10, and splits x*s = hi + lo with hi an integer (|hi| <=
+//     1024, exact in fp16) and lo (|lo| <= 1/2) rounded to fp16;
 //   * the host splits 1024 * B the same way into an integer matrix Bh and
-//     an fp16 residual Bl (|1024 * B - Bh| <= 1/2, stored times 2^11);
+//     an fp16 residual Bl = 1024 * B - Bh (|Bl| <= 1/2);
 //   * D1 = hi * Bh is a sum of integer products bounded by
 //     1024 * (1024 * 8 + 32) < 2^24 (a unitary's real-form columns have
 //     L1 norm <= 8), so every partial sum is an exact FP32 integer and the
 //     truncating accumulator makes no error;
-//   * D2 = lo * Bh + hi * Bl (three-product split, Ootomo & Yokota 2022)
-//     carries the correction at 2^-11 of D1's scale, where truncation
-//     costs about 2^-35 relative;
-//   * y = (D1 + D2 * 2^-11) / (1024 s), exact power-of-two scalings.
+//   * Dc = hi * Bl + lo * Bh (the three-product split of Ootomo & Yokota
+//     2022, as one K = 128 product [hi | lo] * [Bl; Bh]) carries the
+//     correction, about 2^-11 of D1's magnitude, where the truncation
+//     costs about 2^-34 relative;
+//   * y = (D1 + Dc) / (1024 s), an exact power-of-two scaling.
 // The representation error is about 2^-22 of each column's largest
 // amplitude per block.
 //
 // Diagonal gates whose bits are all outside a block's bits (thread bits,
-// or positions outside the tile) commute with the block: the planner
-// attaches them to the block as "post-diagonals", folded into a per-thread
-// factor applied when the block's result is written back.
+// or positions outside the tile) commute with the block.  The host folds
+// them into a per-block table of per-thread factors indexed by up to 5 bits
+// outside the tile; the rare rest stay a list of post-diagonals.
 //
-// Pipeline (two CTAs of 128 threads per SM, 97 KiB of shared memory and
-// 256 tensor-memory columns each): the next tile streams in by 16-byte
-// cp.async while the current tile's blocks run; block matrices (16 KiB
-// images: fp16 Bh then Bl, in the canonical K-major no-swizzle layout) are
-// resident when a stage has at most two blocks and otherwise stream through
-// two buffers by cp.async.bulk, one block ahead.  While one CTA waits for
-// its MMAs the other gathers, splits or scatters.  Every wait on an
-// mbarrier is bounded; a wait that runs out records an error (read with
-// gbsv_tc_status), drains what is in flight and ends the CTA.
+// Work is split by role (two CTAs of 192 threads per SM, 107 KiB of shared
+// memory and 256 tensor-memory columns each): four compute warps (gather,
+// split, tcgen05.st, tcgen05.ld, scatter), one warp whose lane 0 issues the
+// MMAs and streams block images (16 KiB, resident when a stage has at most
+// two blocks, otherwise two buffers by cp.async.bulk), and one warp that
+// loads tiles by 16-byte cp.async into two buffers and writes finished
+// tiles back, so the memory pipeline never stalls the compute warps.
 #include "common.cuh"
 
 #include <cuda_fp16.h>
@@ -64,8 +63,8 @@ constexpr int TC_TB = TC_M - TC_RB;  // thread bits
 constexpr int TC_THREADS = 1 << TC_TB;
 constexpr int TC_TILE = 1 << TC_M;
 constexpr int TC_MAX_BLOCKS = 64;
+constexpr int TC_MAX_SDIAG = 64;     // post-diagonals staged in shared memory
 constexpr int TC_IMG_BYTES = 16384;
-constexpr int TC_IMG_HALF = 8192;
 constexpr int TC_SMEM_BYTES = 2 * TC_TILE * 8 + 2 * TC_IMG_BYTES + 1024;
 
 // Block record (gbsv_tc_block_t).  Shared-memory offsets are in amplitudes
@@ -73,12 +72,16 @@ constexpr int TC_SMEM_BYTES = 2 * TC_TILE * 8 + 2 * TC_IMG_BYTES + 1024;
 // (thread bits of r) | (register bits of i) sits at
 // XOR(tspo[j] : bit j of r) ^ XOR(rspo[k] : bit k of i).
 struct TcBlock {
-  int32_t rspo[TC_RB];  // register-index bit k -> swizzled offset
-  int32_t tspo[TC_TB];  // thread-index bit j -> swizzled offset
+  int16_t rspo[TC_RB];  // register-index bit k -> swizzled offset
+  int16_t tspo[TC_TB];  // thread-index bit j -> swizzled offset
   int32_t mat;          // image index (16 KiB each)
   int32_t first_diag;   // post-diagonals [first_diag, first_diag + num_diag)
   int32_t num_diag;
   int32_t flags;        // TC_PAIRS: register bit 0 is tile bit 0
+  int32_t fac;          // factor table: factors[fac + p * 128 + thread]
+  int8_t nout;          // p's bits: the state's bits at positions opos[]
+  int8_t opos[7];
+  int32_t pad_[3];
 };
 static_assert(sizeof(TcBlock) == 64, "gbsv_tc_block_t is 64 bytes");
 constexpr int TC_PAIRS = 1;
@@ -103,6 +106,7 @@ struct TcArgs {
   const TcBlock* blocks;
   const TcDiag* diags;
   const unsigned char* images;
+  const float2* factors;
 };
 
 static __device__ int g_tc_status;  // nonzero after a bounded wait ran out
@@ -112,6 +116,11 @@ static __device__ int g_tc_status;  // nonzero after a bounded wait ran out
 // tile bit >= 1 has a non-zero image in the bank bits.
 __device__ __forceinline__ int tc_swz(int l) {
   return l ^ ((((l >> 4) ^ (l >> 7) ^ (l >> 10)) & 7) << 1);
+}
+
+// Lowest set bit of a (compile-time) register index.
+__host__ __device__ constexpr int tc_ctz(int i) {
+  return (i & 1) ? 0 : (i & 2) ? 1 : (i & 4) ? 2 : (i & 8) ? 3 : 4;
 }
 
 __device__ __forceinline__ uint32_t tc_smem(const void* p) {
@@ -150,18 +159,19 @@ __device__ __forceinline__ void tc_load_image(uint32_t dst, const void* src,
 
 // Shared-memory matrix descriptor: K-major, no swizzle; core matrices of
 // 8 rows x 16 bytes, K-adjacent ones 128 bytes apart (leading byte offset),
-// 8-row groups 1024 bytes apart (stride byte offset).
+// 8-row groups 2048 bytes apart (stride byte offset).
 __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
   return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) |
-         ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46);
+         ((uint64_t)(2048 >> 4) << 32) | ((uint64_t)1 << 46);
 }
 
 // D (f32) = A (f16, tensor memory) * B (f16, shared memory), M = 128,
-// N = 64, K = 16; accumulate into D when acc != 0.
+// N = 64 or 128, K = 16; accumulate into D when acc != 0.
+template <int N>
 __device__ __forceinline__ void tc_mma(uint32_t d, uint32_t a, uint64_t b,
                                        uint32_t acc) {
   constexpr uint32_t idesc = (1u << 4)  // D f32; A, B f16; both K-major
-                             | ((uint32_t)(64 >> 3) << 17) |
+                             | ((uint32_t)(N >> 3) << 17) |
                              ((uint32_t)(128 >> 4) << 24);
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
@@ -171,13 +181,20 @@ __device__ __forceinline__ void tc_mma(uint32_t d, uint32_t a, uint64_t b,
       : "memory");
 }
 
-#define TC_R32(r)                                                            \
+#define TC_R16(r)                                                            \
   "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]),          \
       "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]),    \
-      "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]),            \
-      "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]),            \
-      "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]),            \
-      "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
+      "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+
+// 16 consecutive 32-bit columns of this thread's lane.
+__device__ __forceinline__ void tc_st16(uint32_t taddr, const uint32_t* r) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
+      TC_R16(r)
+      : "memory");
+}
+
 #define TC_W32(r)                                                            \
   "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),    \
       "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]),           \
@@ -186,26 +203,14 @@ __device__ __forceinline__ void tc_mma(uint32_t d, uint32_t a, uint64_t b,
       "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),       \
       "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),       \
       "=r"(r[31])
-#define TC_LIST32                                                            \
-  "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20," \
-  "%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32}"
-#define TC_LIST32_OUT                                                        \
-  "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"  \
-  "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}"
-
-// 32 consecutive 32-bit columns of this thread's lane.
-__device__ __forceinline__ void tc_st32(uint32_t taddr, const uint32_t* r) {
-  asm volatile("tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], " TC_LIST32
-               ";" ::"r"(taddr),
-               TC_R32(r)
-               : "memory");
-}
 __device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t* r) {
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 " TC_LIST32_OUT
-               ", [%32];"
-               : TC_W32(r)
-               : "r"(taddr)
-               : "memory");
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+      "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : TC_W32(r)
+      : "r"(taddr)
+      : "memory");
 }
 
 __device__ __forceinline__ uint32_t tc_pack(float lo_k, float hi_k) {
@@ -231,7 +236,31 @@ __device__ __forceinline__ uint64_t tc_tile_offset(const TcArgs& a, int l) {
   return off;
 }
 
-__global__ void __launch_bounds__(TC_THREADS, 1)
+// Roles (192 threads): warps 0-3 compute (thread r owns column r of the
+// tile and TMEM lane r), warp 4 lane 0 issues the MMAs and streams block
+// images, warp 5 loads and stores tiles.  They hand over through mbarriers:
+//   full[b]   tile buffer b loaded      (warp 5 cp.async -> compute)
+//   empty[b]  tile buffer b computed    (compute -> warp 5: store, refill)
+//   a_ready   A written to TMEM         (compute -> MMA lane)
+//   mma_done  MMAs of a block complete  (tcgen05.commit -> compute)
+//   img[b]    block image b landed      (cp.async.bulk -> MMA lane)
+// Every wait is bounded (tc_wait); one that runs out sets the CTA's abort
+// flag and the error status, and every role then leaves its loop.
+constexpr int TC_ROLE_THREADS = TC_THREADS + 64;
+
+// Barrier 1 over the compute warps, returning the OR of x over them.
+__device__ __forceinline__ bool tc_compute_sync_or(bool x) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.or.pred q, 1, %2, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)x), "n"(TC_THREADS)
+      : "memory");
+  return r != 0;
+}
+
+__global__ void __launch_bounds__(TC_ROLE_THREADS, 2)
     tc_stage_kernel(const float2* in, float2* out, TcArgs a) {
   extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
   // 1024-byte alignment of the dynamic area is not guaranteed: round up
@@ -240,19 +269,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   float2* const tiles = reinterpret_cast<float2*>(smem);
   unsigned char* const imgs = smem + 2 * TC_TILE * 8;
   __shared__ TcBlock sblk[TC_MAX_BLOCKS];
+  __shared__ TcDiag sdiag[TC_MAX_SDIAG];
   __shared__ uint64_t offh[16];
-  __shared__ __align__(8) uint64_t mbar_img[2];
-  __shared__ __align__(8) uint64_t mbar_mma;
+  __shared__ __align__(8) uint64_t bar_full[2], bar_empty[2], bar_img[2];
+  __shared__ __align__(8) uint64_t bar_a, bar_mma;
   __shared__ uint32_t s_tmem;
+  __shared__ volatile int s_abort;
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
+  const int lane_id = tid & 31;
   const int nb = a.num_blocks;
   const uint64_t tps = uint64_t(1) << (a.n - TC_M);
   const uint64_t num_tiles = (uint64_t)a.num_states * tps;
   const uint64_t t0 = (uint64_t)blockIdx.x * num_tiles / gridDim.x;
   const uint64_t t1 = (uint64_t)(blockIdx.x + 1) * num_tiles / gridDim.x;
   if (t0 >= t1) return;
+  const uint64_t ntile = t1 - t0;
+  const uint64_t total_exec = ntile * (uint64_t)nb;
 
   if (warp == 0) {
     asm volatile(
@@ -264,261 +298,353 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             : "memory");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(
-        tc_smem(&mbar_img[0])));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(
-        tc_smem(&mbar_img[1])));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(
-        tc_smem(&mbar_mma)));
+    auto init = [](uint64_t* bar, int count) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(
+                       tc_smem(bar)),
+                   "r"(count));
+    };
+    init(&bar_full[0], 32);  // one cp.async arrival per loader lane
+    init(&bar_full[1], 32);
+    init(&bar_empty[0], TC_THREADS);
+    init(&bar_empty[1], TC_THREADS);
+    init(&bar_img[0], 1);
+    init(&bar_img[1], 1);
+    init(&bar_a, TC_THREADS);
+    init(&bar_mma, 1);
+    s_abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (int i = tid; i < nb * 16; i += TC_THREADS)
+  for (int i = tid; i < nb * 16; i += TC_ROLE_THREADS)
     reinterpret_cast<int32_t*>(sblk)[i] =
         reinterpret_cast<const int32_t*>(a.blocks)[i];
+  // the stage's post-diagonals: one contiguous range, staged in shared
+  // memory when it fits (read from global memory otherwise)
+  const int dfirst = a.blocks[0].first_diag;
+  const int dcount =
+      a.blocks[nb - 1].first_diag + a.blocks[nb - 1].num_diag - dfirst;
+  const bool dshared = dcount <= TC_MAX_SDIAG;
+  if (dshared)
+    for (int i = tid; i < dcount * 12; i += TC_ROLE_THREADS)
+      reinterpret_cast<int32_t*>(sdiag)[i] =
+          reinterpret_cast<const int32_t*>(a.diags + dfirst)[i];
+  const TcDiag* const dtab = dshared ? sdiag - dfirst : a.diags;
   if (tid < 16) offh[tid] = tc_tile_offset(a, 256 * tid);
-  const uint64_t offt = tc_tile_offset(a, 2 * tid);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = s_tmem;
-  const uint32_t lane = (uint32_t)(warp * 32) << 16;
-  const uint32_t tA_hi = tmem, tA_lo = tmem + 32, tD1 = tmem + 64,
-                 tD2 = tmem + 128;
 
-  // block-matrix images: resident (nb <= 2) or streamed one exec ahead
-  const bool resident = nb <= 2;
-  const uint64_t total_exec = (t1 - t0) * (uint64_t)nb;
-  uint32_t img_phase = 0;   // bit b: parity of the next load into buffer b
-  int img_pending = 0;      // loads issued and not yet waited (tid 0)
-  if (tid == 0) {
-    const int first = resident ? nb : (total_exec < 2 ? (int)total_exec : 2);
-    for (int e = 0; e < first; ++e) {
-      tc_load_image(tc_smem(imgs + e * TC_IMG_BYTES),
-                    a.images + (size_t)sblk[e % nb].mat * TC_IMG_BYTES,
-                    tc_smem(&mbar_img[e]));
-      img_pending |= 1 << e;
-    }
-  }
-
-  auto prefetch = [&](uint64_t t, float2* S) {
-    const uint64_t s = t / tps;
-    const float2* src =
-        in + (int64_t)s * a.in_stride + tc_tile_base(a, t % tps) + offt;
-#pragma unroll
-    for (int it = 0; it < 16; ++it) {
-      const int l = 2 * (tid + TC_THREADS * it);
-      cp_async16<float>(&S[tc_swz(l)], src + offh[it]);
-    }
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  // tiles of a CTA are consecutive: the base (the tile's amplitude bits
+  // outside the tile) steps by a masked increment over the outside bits
+  uint64_t tmask = ~((uint64_t(1) << a.n) - 1);
+  for (int j = 0; j < TC_M; ++j) tmask |= uint64_t(1) << a.spos[j];
+  auto next_base = [&](uint64_t b) { return ((b | tmask) + 1) & ~tmask; };
+  auto fail = [&](int code) {
+    s_abort = 1;
+    atomicOr(&g_tc_status, code);
   };
 
-  prefetch(t0, tiles);
-  uint32_t mma_phase = 0;
-  uint64_t e = 0;  // block executions so far
-  bool bad = false;
-  bool mma_late = false;  // an MMA wait ran out
-  for (uint64_t t = t0; t < t1 && !bad; ++t) {
-    float2* const S = tiles + (int)((t - t0) & 1) * TC_TILE;
+  if (warp == 5) {
+    // ---------------------------------------------- tile loader / storer
+    // lane l moves 16-byte pieces l, l + 32, ... (amplitudes 2 * piece);
+    // piece p = 32 i + l has tile index 2p = 64 i + 2 l
+    const uint64_t offl = tc_tile_offset(a, 2 * lane_id);
+    uint64_t offs[4];  // 64 i = 256 (i >> 2) + 64 (i & 3)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) offs[q] = tc_tile_offset(a, 64 * q) + offl;
+    auto load = [&](uint64_t s, uint64_t base, int b) {
+      float2* S = tiles + b * TC_TILE;
+      const float2* src = in + (int64_t)s * a.in_stride + base;
+#pragma unroll 8
+      for (int i = 0; i < 64; ++i) {
+        const int l = 64 * i + 2 * lane_id;
+        cp_async16<float>(&S[tc_swz(l)], src + offh[i >> 2] + offs[i & 3]);
+      }
+      asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::
+                       "r"(tc_smem(&bar_full[b]))
+                   : "memory");
+    };
+    uint64_t s = t0 / tps, base = tc_tile_base(a, t0 % tps);
+    uint64_t ls = s, lbase = base;  // next tile to load
+    for (uint64_t k = 0; k < 2 && k < ntile; ++k) {
+      load(ls, lbase, (int)k);
+      lbase = next_base(lbase);
+      ls += lbase == 0;
+    }
+    for (uint64_t k = 0; k < ntile; ++k) {
+      const int b = (int)(k & 1);
+      if (!tc_wait(tc_smem(&bar_empty[b]), (uint32_t)((k >> 1) & 1))) {
+        fail(16);
+        break;
+      }
+      const float2* S = tiles + b * TC_TILE;
+      float2* dst = out + (s << a.n) + base;
+#pragma unroll 8
+      for (int i = 0; i < 64; ++i) {
+        const int l = 64 * i + 2 * lane_id;
+        const float4 w = *reinterpret_cast<const float4*>(&S[tc_swz(l)]);
+        __stcs(reinterpret_cast<float4*>(dst + offh[i >> 2] + offs[i & 3]),
+               w);
+      }
+      __syncwarp();  // every lane's reads done before the buffer refills
+      if (k + 2 < ntile) {
+        load(ls, lbase, b);
+        lbase = next_base(lbase);
+        ls += lbase == 0;
+      }
+      base = next_base(base);
+      s += base == 0;
+      if (s_abort) break;
+    }
     cp_async_wait_all();
-    __syncthreads();
-    if (t + 1 < t1) prefetch(t + 1, tiles + (int)((t + 1 - t0) & 1) * TC_TILE);
-    const uint64_t s = t / tps;
-    const uint64_t base = tc_tile_base(a, t % tps);
-
-    for (int bi = 0; bi < nb; ++bi, ++e) {
-      const TcBlock& B = sblk[bi];
-      int sb = 0;
-#pragma unroll
-      for (int j = 0; j < TC_TB; ++j)
-        if ((tid >> j) & 1) sb ^= B.tspo[j];
-      int rs[TC_RB];
-#pragma unroll
-      for (int k = 0; k < TC_RB; ++k) rs[k] = B.rspo[k];
-      auto roff = [&](int i) {
-        int x = sb;
-#pragma unroll
-        for (int k = 0; k < TC_RB; ++k)
-          if ((i >> k) & 1) x ^= rs[k];
-        return x;
-      };
-      const bool pairs = B.flags & TC_PAIRS;
-
-      // gather column tid
-      float2 v[32];
-      if (pairs) {
-#pragma unroll
-        for (int i = 0; i < 32; i += 2) {
-          const float4 w = *reinterpret_cast<const float4*>(&S[roff(i)]);
-          v[i] = make_float2(w.x, w.y);
-          v[i + 1] = make_float2(w.z, w.w);
-        }
-      } else {
-#pragma unroll
-        for (int i = 0; i < 32; ++i) v[i] = S[roff(i)];
+  } else if (warp == 4) {
+    // -------------------------------------------------------- MMA issuer
+    if (lane_id == 0) {
+      const bool resident = nb <= 2;
+      uint32_t img_phase = 0;  // bit b: parity of the next wait on img[b]
+      int img_pending = 0;
+      const int first = resident ? nb : (total_exec < 2 ? (int)total_exec : 2);
+      for (int e = 0; e < first; ++e) {
+        tc_load_image(tc_smem(imgs + e * TC_IMG_BYTES),
+                      a.images + (size_t)sblk[e % nb].mat * TC_IMG_BYTES,
+                      tc_smem(&bar_img[e]));
+        img_pending |= 1 << e;
       }
-
-      // power-of-two scaling and the exact-integer / residual split
-      uint32_t emax = 0;
-#pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        emax = max(emax, __float_as_uint(v[i].x) & 0x7f800000u);
-        emax = max(emax, __float_as_uint(v[i].y) & 0x7f800000u);
-      }
-      const int E = max((int)(emax >> 23), 20);
-      const float sc = __uint_as_float((uint32_t)(263 - E) << 23);  // 2^(136-E)
-      const float sc2 = sc * 2048.f;
-      const float inv = __uint_as_float((uint32_t)(E - 19) << 23);  // 2^(E-146)
-      {
-        uint32_t hi[32], lo[32];
-#pragma unroll
-        for (int i = 0; i < 32; ++i) {
-          const float hr = rintf(v[i].x * sc), hm = rintf(v[i].y * sc);
-          const float lr = fmaf(v[i].x, sc2, -2048.f * hr);
-          const float lm = fmaf(v[i].y, sc2, -2048.f * hm);
-          hi[i] = tc_pack(hr, hm);
-          lo[i] = tc_pack(lr, lm);
-        }
-        tc_st32(tA_hi + lane, hi);
-        tc_st32(tA_lo + lane, lo);
-      }
-      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncthreads();
-
-      if (tid == 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      for (uint64_t e = 0; e < total_exec; ++e) {
+        const int bi = (int)(e % nb);
         const int buf = resident ? bi : (int)(e & 1);
+        if (!tc_wait(tc_smem(&bar_a), (uint32_t)(e & 1))) {
+          fail(32);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         bool ok = true;
         if ((img_pending >> buf) & 1) {
-          ok = tc_wait(tc_smem(&mbar_img[buf]), (img_phase >> buf) & 1);
+          ok = tc_wait(tc_smem(&bar_img[buf]), (img_phase >> buf) & 1);
           img_pending &= ~(1 << buf);
           img_phase ^= 1u << buf;
         }
         if (ok) {
-          const uint32_t bh = tc_smem(imgs + buf * TC_IMG_BYTES);
-          const uint32_t bl = bh + TC_IMG_HALF;
+          // image: [Bl; Bh] as a K = 128 x N = 64 operand (8-row groups
+          // 2048 bytes apart); Bh alone starts 1024 bytes in
+          const uint32_t im = tc_smem(imgs + buf * TC_IMG_BYTES);
 #pragma unroll
           for (int j = 0; j < 4; ++j)
-            tc_mma(tD1, tA_hi + 8 * j, tc_desc(bh + 256 * j), j > 0);
+            tc_mma<64>(tmem + 64, tmem + 8 * j, tc_desc(im + 1024 + 256 * j),
+                       j > 0);
 #pragma unroll
-          for (int j = 0; j < 4; ++j)
-            tc_mma(tD2, tA_lo + 8 * j, tc_desc(bh + 256 * j), j > 0);
-#pragma unroll
-          for (int j = 0; j < 4; ++j)
-            tc_mma(tD2, tA_hi + 8 * j, tc_desc(bl + 256 * j), 1);
+          for (int j = 0; j < 8; ++j)
+            tc_mma<64>(tmem + 128, tmem + 8 * j, tc_desc(im + 256 * j), j > 0);
         } else {
-          atomicOr(&g_tc_status, 1);
+          fail(1);
         }
         // commit even after a failed wait: it then arrives at once
         asm volatile(
             "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::"
-            "cluster.b64 [%0];" ::"r"(tc_smem(&mbar_mma))
+            "cluster.b64 [%0];" ::"r"(tc_smem(&bar_mma))
             : "memory");
-        bad |= !ok;
+        if (!ok) break;
+        if (!resident && e + 2 < total_exec) {
+          // image buffer `buf` is free once these MMAs complete
+          if (!tc_wait(tc_smem(&bar_mma), (uint32_t)(e & 1))) {
+            fail(2);
+            break;
+          }
+          tc_load_image(
+              tc_smem(imgs + buf * TC_IMG_BYTES),
+              a.images + (size_t)sblk[(int)((e + 2) % nb)].mat * TC_IMG_BYTES,
+              tc_smem(&bar_img[buf]));
+          img_pending |= 1 << buf;
+        }
+        if (s_abort) break;
       }
-      if (!tc_wait(tc_smem(&mbar_mma), mma_phase)) {
+      for (int b = 0; b < 2; ++b)
+        if ((img_pending >> b) & 1)
+          if (!tc_wait(tc_smem(&bar_img[b]), (img_phase >> b) & 1)) fail(4);
+    }
+  } else {
+    // ---------------------------------------------------------- compute
+    const uint32_t lane = (uint32_t)(warp * 32) << 16;
+    const uint32_t tA = tmem, tD1 = tmem + 64, tDc = tmem + 128;
+    uint64_t s = t0 / tps, base = tc_tile_base(a, t0 % tps);
+    // A wait that runs out only sets `bad`: every compute thread runs the
+    // same tcgen05 and barrier sequence, and all leave together after the
+    // reduction barrier that ends each block.
+    uint64_t e = 0;
+    bool bad = false;
+    bool late = false;  // an MMA completion wait ran out
+    for (uint64_t k = 0; k < ntile && !bad; ++k) {
+      const int b = (int)(k & 1);
+      float2* const S = tiles + b * TC_TILE;
+      if (!tc_wait(tc_smem(&bar_full[b]), (uint32_t)((k >> 1) & 1))) {
+        fail(64);
         bad = true;
-        mma_late = true;
-        atomicOr(&g_tc_status, 2);
       }
-      mma_phase ^= 1;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      // the image buffer of this execution is free: stream the one after
-      // next into it
-      if (tid == 0 && !resident && !bad && e + 2 < total_exec) {
-        const int buf = (int)(e & 1);
-        tc_load_image(tc_smem(imgs + buf * TC_IMG_BYTES),
-                      a.images +
-                          (size_t)sblk[(int)((e + 2) % nb)].mat * TC_IMG_BYTES,
-                      tc_smem(&mbar_img[buf]));
-        img_pending |= 1 << buf;
-      }
-
-      // per-thread factor of the post-diagonals on thread / outside bits
-      float2 f = make_float2(inv, 0.f);
-      bool regdiag = false;
-      for (int q = B.first_diag; q < B.first_diag + B.num_diag; ++q) {
-        const TcDiag& dg = a.diags[q];
-        if (dg.reg) {
-          regdiag = true;
-          continue;
-        }
-        int idx = 0;
-        for (int u = 0; u < dg.nq; ++u) {
-          const int en = dg.enc[u];
-          const int bit = en >= TC_RB ? (tid >> (en - TC_RB)) & 1
-                                      : (int)((base >> (-1 - en)) & 1);
-          idx = (idx << 1) | bit;
-        }
-        f = cmul(f, dg.d[idx]);
-      }
-      // read back D1, D2 and combine
+      for (int bi = 0; bi < nb; ++bi, ++e) {
+        const TcBlock& B = sblk[bi];
+        int sb = 0;
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        uint32_t d1[32], d2[32];
-        tc_ld32(tD1 + lane + 32 * h, d1);
-        tc_ld32(tD2 + lane + 32 * h, d2);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        for (int j = 0; j < TC_TB; ++j)
+          if ((tid >> j) & 1) sb ^= B.tspo[j];
+        int rs[TC_RB];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const float re = fmaf(__uint_as_float(d2[2 * j]), 1.f / 2048.f,
-                                __uint_as_float(d1[2 * j]));
-          const float im = fmaf(__uint_as_float(d2[2 * j + 1]), 1.f / 2048.f,
-                                __uint_as_float(d1[2 * j + 1]));
-          v[16 * h + j] = cmul(f, make_float2(re, im));
+        for (int j = 0; j < TC_RB; ++j) rs[j] = B.rspo[j];
+        const bool pairs = B.flags & TC_PAIRS;
+        // this thread's factor of the diagonals folded into the block's
+        // table, loaded now and used after the MMAs
+        float2 fv = make_float2(1.f, 0.f);
+        const int fac = B.fac;
+        if (fac >= 0) {
+          int p = 0;
+          for (int j = 0; j < B.nout; ++j)
+            p |= (int)((base >> B.opos[j]) & 1) << j;
+          fv = __ldg(a.factors + fac + p * TC_THREADS + tid);
         }
-      }
-      if (regdiag) {
+        // register i lives at sb ^ (XOR of rs[j] over the bits j of i)
+        int ad[32];
+        auto addresses = [&]() {
+          ad[0] = sb;
+#pragma unroll
+          for (int i = 1; i < 32; ++i)
+            ad[i] = ad[i & (i - 1)] ^ rs[tc_ctz(i)];
+        };
+        addresses();
+        float2 v[32];
+        if (pairs) {
+#pragma unroll
+          for (int i = 0; i < 32; i += 2) {
+            const float4 w = *reinterpret_cast<const float4*>(&S[ad[i]]);
+            v[i] = make_float2(w.x, w.y);
+            v[i + 1] = make_float2(w.z, w.w);
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < 32; ++i) v[i] = S[ad[i]];
+        }
+        // power-of-two scaling (largest |x| of the column, tree reduction)
+        float mx[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+          mx[i] = fmaxf(fmaxf(fabsf(v[i].x), fabsf(v[i].y)),
+                        fmaxf(fabsf(v[i + 16].x), fabsf(v[i + 16].y)));
+#pragma unroll
+        for (int w = 8; w > 0; w >>= 1)
+#pragma unroll
+          for (int i = 0; i < w; ++i) mx[i] = fmaxf(mx[i], mx[i + w]);
+        const int E = max((int)(__float_as_uint(mx[0]) >> 23), 20);
+        const float sc = __uint_as_float((uint32_t)(263 - E) << 23);
+        const float inv = __uint_as_float((uint32_t)(E - 19) << 23);
+        // x * sc = hi + lo: hi = x * sc rounded to an integer (adding and
+        // removing 1.5 * 2^23 rounds to nearest; |x * sc| < 2^10), lo the
+        // exact remainder (|lo| <= 1/2), both to fp16
+        constexpr float RND = 12582912.f;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          uint32_t hi[16], lo[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const float2 x = v[16 * h + j];
+            const float hr = fmaf(x.x, sc, RND) - RND;
+            const float hm = fmaf(x.y, sc, RND) - RND;
+            hi[j] = tc_pack(hr, hm);
+            lo[j] = tc_pack(fmaf(x.x, sc, -hr), fmaf(x.y, sc, -hm));
+          }
+          tc_st16(tA + lane + 16 * h, hi);
+          tc_st16(tA + 32 + lane + 16 * h, lo);
+        }
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
+                         tc_smem(&bar_a))
+                     : "memory");
+        // post-diagonals left in the list (a register bit, or too many
+        // outside bits), while the MMAs run
+        float2 f = make_float2(fv.x * inv, fv.y * inv);
+        bool regdiag = false;
+        const bool has_diag = B.num_diag > 0 || fac >= 0;
         for (int q = B.first_diag; q < B.first_diag + B.num_diag; ++q) {
-          const TcDiag& dg = a.diags[q];
-          if (!dg.reg) continue;
+          const TcDiag& dg = dtab[q];
+          if (dg.reg) {
+            regdiag = true;
+            continue;
+          }
+          int idx = 0;
+          for (int u = 0; u < dg.nq; ++u) {
+            const int en = dg.enc[u];
+            const int bit = en >= TC_RB ? (tid >> (en - TC_RB)) & 1
+                                        : (int)((base >> (-1 - en)) & 1);
+            idx = (idx << 1) | bit;
+          }
+          f = cmul(f, dg.d[idx]);
+        }
+        if (!tc_wait(tc_smem(&bar_mma), (uint32_t)(e & 1))) {
+          fail(2);
+          late = true;
+          bad = true;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // read back D1 + Dc, undo the scaling, apply the factors
 #pragma unroll
-          for (int i = 0; i < 32; ++i) {
-            int idx = 0;
-            for (int u = 0; u < dg.nq; ++u) {
-              const int en = dg.enc[u];
-              const int bit = en < 0 ? (int)((base >> (-1 - en)) & 1)
-                              : en < TC_RB ? (i >> en) & 1
-                                           : (tid >> (en - TC_RB)) & 1;
-              idx = (idx << 1) | bit;
-            }
-            v[i] = cmul(dg.d[idx], v[i]);
+        for (int h = 0; h < 2; ++h) {
+          uint32_t d1[32], dc[32];
+          tc_ld32(tD1 + lane + 32 * h, d1);
+          tc_ld32(tDc + lane + 32 * h, dc);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const float re =
+                __uint_as_float(d1[2 * j]) + __uint_as_float(dc[2 * j]);
+            const float im = __uint_as_float(d1[2 * j + 1]) +
+                             __uint_as_float(dc[2 * j + 1]);
+            v[16 * h + j] = has_diag ? cmul(f, make_float2(re, im))
+                                     : make_float2(re * inv, im * inv);
           }
         }
-      }
-      // scatter back (the same addresses the gather read)
-      if (pairs) {
+        if (regdiag) {
+          for (int q = B.first_diag; q < B.first_diag + B.num_diag; ++q) {
+            const TcDiag& dg = dtab[q];
+            if (!dg.reg) continue;
 #pragma unroll
-        for (int i = 0; i < 32; i += 2)
-          *reinterpret_cast<float4*>(&S[roff(i)]) =
-              make_float4(v[i].x, v[i].y, v[i + 1].x, v[i + 1].y);
-      } else {
+            for (int i = 0; i < 32; ++i) {
+              int idx = 0;
+              for (int u = 0; u < dg.nq; ++u) {
+                const int en = dg.enc[u];
+                const int bit = en < 0 ? (int)((base >> (-1 - en)) & 1)
+                                : en < TC_RB ? (i >> en) & 1
+                                             : (tid >> (en - TC_RB)) & 1;
+                idx = (idx << 1) | bit;
+              }
+              v[i] = cmul(dg.d[idx], v[i]);
+            }
+          }
+        }
+        // scatter back (the same addresses the gather read)
+        addresses();
+        if (pairs) {
 #pragma unroll
-        for (int i = 0; i < 32; ++i) S[roff(i)] = v[i];
+          for (int i = 0; i < 32; i += 2)
+            *reinterpret_cast<float4*>(&S[ad[i]]) =
+                make_float4(v[i].x, v[i].y, v[i + 1].x, v[i + 1].y);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 32; ++i) S[ad[i]] = v[i];
+        }
+        // the next block reads other threads' results; errors anywhere
+        // stop every compute thread here
+        bad = tc_compute_sync_or(bad || s_abort);
+        if (bad) break;
       }
-      bad = __syncthreads_or(bad);
       if (bad) break;
+      // this thread's part of the tile is final: the storer may take it
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
+                       tc_smem(&bar_empty[b]))
+                   : "memory");
+      base = next_base(base);
+      s += base == 0;
     }
-    if (bad) break;
-
-    float2* dst = out + (s << a.n) + base + offt;
-#pragma unroll
-    for (int it = 0; it < 16; ++it) {
-      const int l = 2 * (tid + TC_THREADS * it);
-      const float4 w = *reinterpret_cast<const float4*>(&S[tc_swz(l)]);
-      __stcs(reinterpret_cast<float4*>(dst + offh[it]), w);
-    }
+    if (late && !tc_wait(tc_smem(&bar_mma), (uint32_t)((e & 1)))) fail(8);
   }
-  // drain: tile copies, image loads and MMAs in flight
-  cp_async_wait_all();
-  if (mma_late && !tc_wait(tc_smem(&mbar_mma), mma_phase ^ 1))
-    atomicOr(&g_tc_status, 8);
-  if (tid == 0) {
-    for (int b = 0; b < 2; ++b)
-      if ((img_pending >> b) & 1)
-        if (!tc_wait(tc_smem(&mbar_img[b]), (img_phase >> b) & 1))
-          atomicOr(&g_tc_status, 4);
-  }
+  // every role is done (waits are bounded): free tensor memory
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) {
@@ -539,7 +665,7 @@ extern "C" int gbsv_run_stage_tc(const void* state_in, void* state_out,
                                  const int32_t* positions,
                                  const void* blocks, int num_blocks,
                                  const void* diags, const void* images,
-                                 void* stream) {
+                                 const void* factors, void* stream) {
   using namespace gbsv;
   if (dtype != GBSV_C64)
     return set_error(GBSV_ERR_UNSUPPORTED,
@@ -592,6 +718,7 @@ extern "C" int gbsv_run_stage_tc(const void* state_in, void* state_out,
   a.blocks = static_cast<const TcBlock*>(blocks);
   a.diags = static_cast<const TcDiag*>(diags);
   a.images = static_cast<const unsigned char*>(images);
+  a.factors = static_cast<const float2*>(factors);
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(tc_stage_kernel,
@@ -602,7 +729,7 @@ extern "C" int gbsv_run_stage_tc(const void* state_in, void* state_out,
   const uint64_t tiles =
       (uint64_t)num_states << (n - TC_M);
   const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)sm_count() * 2);
-  tc_stage_kernel<<<(unsigned)grid, TC_THREADS, TC_SMEM_BYTES,
+  tc_stage_kernel<<<(unsigned)grid, TC_ROLE_THREADS, TC_SMEM_BYTES,
                     static_cast<cudaStream_t>(stream)>>>(
       static_cast<const float2*>(state_in), static_cast<float2*>(state_out),
       a);

@@ -618,7 +618,7 @@ class Program:
         """Tensor-core stages (tcplan) and single-gate launches."""
         from . import tcplan
         dev = self.device
-        blocks, diags, images = [], [], []
+        blocks, diags, images, factors = [], [], [], []
         self.ops = []
         for kind, item in raw:
             if kind == "plain":
@@ -626,7 +626,7 @@ class Program:
                 continue
             first = len(blocks)
             c, order = tcplan.encode_stage(item, self.n, blocks, diags,
-                                           images)
+                                           images, factors)
             positions = (ctypes.c_int32 * tcplan.TC_M)(*order)
             self.ops.append(("tc", c, positions, first, len(blocks) - first))
         self.tc_blocks = _to_device(
@@ -635,7 +635,9 @@ class Program:
             np.stack(diags).view(np.uint8) if diags else None, dev)
         self.tc_images = _to_device(
             np.concatenate(images).view(np.uint8) if images else None, dev)
-        self.tc_records = (blocks, diags, images)  # host copies (tests)
+        self.tc_factors = _to_device(
+            np.concatenate(factors).view(np.uint8) if factors else None, dev)
+        self.tc_records = (blocks, diags, images, factors)  # host copies
         self.gate_records = self.layout_records = _to_device(None, dev)
         self.num_layouts = 0
         self.pool = torch.zeros(1, dtype=self.dtype, device=dev)
@@ -790,7 +792,7 @@ class Program:
                 self.m, c, positions,
                 self.tc_blocks.data_ptr() + first * 64, count,
                 self.tc_diags.data_ptr(), self.tc_images.data_ptr(),
-                stream)
+                self.tc_factors.data_ptr(), stream)
             _lib.check(rc, "run_stage_tc")
         elif op[0] == "layouts":
             _, c, positions, first, count = op

@@ -32,14 +32,17 @@ import numpy as np
 TC_M, TC_RB, TC_TB = 12, 5, 7
 TC_MAX_BLOCKS = 64
 TC_PAIRS = 1
-BLOCK_DTYPE = np.dtype([("rspo", "<i4", (5,)), ("tspo", "<i4", (7,)),
+BLOCK_DTYPE = np.dtype([("rspo", "<i2", (5,)), ("tspo", "<i2", (7,)),
                         ("mat", "<i4"), ("first_diag", "<i4"),
-                        ("num_diag", "<i4"), ("flags", "<i4")])
+                        ("num_diag", "<i4"), ("flags", "<i4"), ("fac", "<i4"),
+                        ("nout", "i1"), ("opos", "i1", (7,)),
+                        ("pad", "<i4", (3,))])
+TC_MAX_OUT = 5  # outside bits a block's factor table may depend on
 DIAG_DTYPE = np.dtype([("nq", "<i4"), ("enc", "<i4", (2,)), ("reg", "<i4"),
                        ("d", "<f4", (8,))])
 assert BLOCK_DTYPE.itemsize == 64 and DIAG_DTYPE.itemsize == 48
 IMG_BYTES = 16384
-IMG_ELEMS = IMG_BYTES // 2  # fp16 values per image: Bh then Bl
+IMG_ELEMS = IMG_BYTES // 2  # fp16 values per image: [Bl; Bh]
 
 
 def tc_swz(l: int) -> int:
@@ -48,12 +51,13 @@ def tc_swz(l: int) -> int:
 
 
 def _image_index() -> np.ndarray:
-    """fp16 element index of B[k, n] (64 x 64) in one 8 KiB half-image:
-    core matrices of 8 rows (n) x 16 bytes (8 k), K-adjacent ones 128 bytes
-    apart, 8-row groups 1024 bytes apart."""
-    k = np.arange(64)[:, None]
+    """fp16 element index of the K = 128 x N = 64 operand [Bl; Bh] (rows
+    k < 64 Bl, k >= 64 Bh) in one 16 KiB image: core matrices of 8 rows (n)
+    x 16 bytes (8 k), K-adjacent ones 128 bytes apart, 8-row groups 2048
+    bytes apart."""
+    k = np.arange(128)[:, None]
     n = np.arange(64)[None, :]
-    off = (n % 8) * 16 + (k % 8) * 2 + (k // 8) * 128 + (n // 8) * 1024
+    off = (n % 8) * 16 + (k % 8) * 2 + (k // 8) * 128 + (n // 8) * 2048
     return off // 2
 
 
@@ -153,6 +157,11 @@ def plan_tc(gates: Sequence, n: int, c_min: int = 4):
 
 
 # ----------------------------------------------------------- encoding ----
+def _host_matrix(g) -> np.ndarray:
+    return g.matrix.detach().cpu().resolve_conj().numpy().astype(
+        np.complex128)
+
+
 def _classes(b: int) -> int:
     """Bank-bit image (low 4 amplitude-address bits) of tile bit b."""
     return tc_swz(1 << b) & 15
@@ -198,7 +207,8 @@ def _embed(mat: np.ndarray, kbits: List[int]) -> np.ndarray:
 
 
 def block_image(U: np.ndarray) -> np.ndarray:
-    """fp16 image (8192 values: Bh then Bl) of the real form of U^T."""
+    """fp16 image (8192 values, [Bl; Bh]) of the real form B of U^T:
+    Bh = rint(1024 B) (integers), Bl = 1024 B - Bh."""
     Ur, Ui = U.real, U.imag
     B = np.empty((64, 64))
     B[0::2, 0::2] = Ur.T
@@ -207,24 +217,25 @@ def block_image(U: np.ndarray) -> np.ndarray:
     B[1::2, 1::2] = Ur.T
     Bs = 1024.0 * B
     Bh = np.rint(Bs)
-    Bl = (Bs - Bh) * 2048.0
+    Bl = Bs - Bh
     img = np.zeros(IMG_ELEMS, dtype=np.float16)
-    img[_IMG_IDX] = Bh.astype(np.float16)
-    img[4096 + _IMG_IDX] = Bl.astype(np.float16)
+    img[_IMG_IDX[:64]] = Bl.astype(np.float16)
+    img[_IMG_IDX[64:]] = Bh.astype(np.float16)
     return img
 
 
 def image_matrix(img: np.ndarray) -> np.ndarray:
-    """The real 64x64 matrix B an image stands for (Bh + Bl / 2048) / 1024,
+    """The real 64x64 matrix B an image stands for (Bh + Bl) / 1024,
     as float64 (test helper: what the kernel multiplies by)."""
-    Bh = img[_IMG_IDX].astype(np.float64)
-    Bl = img[4096 + _IMG_IDX].astype(np.float64)
-    return (Bh + Bl / 2048.0) / 1024.0
+    Bl = img[_IMG_IDX[:64]].astype(np.float64)
+    Bh = img[_IMG_IDX[64:]].astype(np.float64)
+    return (Bh + Bl) / 1024.0
 
 
 def encode_stage(plan: TcStagePlan, n: int, blocks_out: list,
-                 diags_out: list, images_out: list):
-    """Records of one stage appended to the program's arrays; returns
+                 diags_out: list, images_out: list, factors_out: list):
+    """Records of one stage appended to the program's arrays (factor tables
+    to factors_out as complex64 arrays of 128 * 2^nout entries); returns
     (c, positions)."""
     tile = set(plan.tile)
     p = 0
@@ -271,29 +282,61 @@ def encode_stage(plan: TcStagePlan, n: int, blocks_out: list,
         U = np.eye(32, dtype=np.complex128)
         for it in blk.gates:
             g = it.gate
-            mat = g.matrix.detach().cpu().resolve_conj().numpy().astype(
-                np.complex128)
+            mat = _host_matrix(g)
             kb = [kpos[n - 1 - q] for q in g.qubits]
             U = _embed(mat, kb) @ U
-        first_diag = len(diags_out)
+        # post-diagonals on thread bits and at most TC_MAX_OUT outside
+        # positions fold into one table of per-thread factors; the rest
+        # (a register bit, or more outside positions) stay a list
+        opos: List[int] = []
+        table_items, listed = [], []
         for it in blk.post:
-            g = it.gate
-            vals = np.diagonal(g.matrix.detach().cpu().resolve_conj().numpy()).astype(
-                np.complex64)
-            rec = np.zeros((), dtype=DIAG_DTYPE)
-            rec["nq"] = len(g.qubits)
-            reg = 0
-            for t, q in enumerate(g.qubits):
+            enc = []
+            for q in it.gate.qubits:
                 pq = n - 1 - q
                 if pq in local:
                     lb = local[pq]
-                    if lb in rb:
-                        rec["enc"][t] = rb.index(lb)
-                        reg = 1
-                    else:
-                        rec["enc"][t] = TC_RB + tb.index(lb)
+                    enc.append(("r", rb.index(lb)) if lb in rb
+                               else ("t", tb.index(lb)))
                 else:
-                    rec["enc"][t] = -1 - pq
+                    enc.append(("o", pq))
+            outs = [v for k, v in enc if k == "o"]
+            new_out = [v for v in dict.fromkeys(outs) if v not in opos]
+            if (all(k != "r" for k, _ in enc)
+                    and len(opos) + len(new_out) <= TC_MAX_OUT):
+                opos += new_out
+                table_items.append((it, enc))
+            else:
+                listed.append((it, enc))
+        fac = -1
+        if table_items:
+            r = np.arange(128)
+            pat = np.arange(2 ** len(opos))
+            tab = np.ones((len(pat), 128), dtype=np.complex128)
+            for it, enc in table_items:
+                vals = np.diagonal(_host_matrix(it.gate))
+                idx = np.zeros((len(pat), 128), dtype=np.int64)
+                for k, v in enc:
+                    bit = (((r >> v) & 1)[None, :] if k == "t" else
+                           ((pat >> opos.index(v)) & 1)[:, None])
+                    idx = (idx << 1) | bit
+                tab = tab * vals[idx]
+            fac = sum(f.size for f in factors_out)
+            factors_out.append(tab.astype(np.complex64).reshape(-1))
+        first_diag = len(diags_out)
+        for it, enc in listed:
+            vals = np.diagonal(_host_matrix(it.gate)).astype(np.complex64)
+            rec = np.zeros((), dtype=DIAG_DTYPE)
+            rec["nq"] = len(enc)
+            reg = 0
+            for t, (k, v) in enumerate(enc):
+                if k == "r":
+                    rec["enc"][t] = v
+                    reg = 1
+                elif k == "t":
+                    rec["enc"][t] = TC_RB + v
+                else:
+                    rec["enc"][t] = -1 - v
             rec["reg"] = reg
             d = np.zeros(8, dtype=np.float32)
             d[0:2 * len(vals):2] = vals.real
@@ -307,6 +350,9 @@ def encode_stage(plan: TcStagePlan, n: int, blocks_out: list,
         brec["first_diag"] = first_diag
         brec["num_diag"] = len(diags_out) - first_diag
         brec["flags"] = TC_PAIRS if pairs else 0
+        brec["fac"] = fac
+        brec["nout"] = len(opos)
+        brec["opos"][:len(opos)] = opos
         images_out.append(block_image(U))
         blocks_out.append(brec)
     return c, order

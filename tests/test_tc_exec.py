@@ -31,7 +31,8 @@ def _apply_plain(psi, mat, qubits, n):
 def run_tc_records(prog, psi, blocks=None):
     """psi (B, 2^n) complex128 -> the program's result, from its records."""
     n = prog.n
-    blocks_l, diags_l, images_l = prog.tc_records
+    blocks_l, diags_l, images_l, factors_l = prog.tc_records
+    factors = np.concatenate(factors_l) if factors_l else np.zeros(0)
     blocks = np.stack(blocks_l) if blocks is None else blocks
     diags = np.stack(diags_l) if diags_l else np.zeros(0, DIAG_DTYPE)
     psi = psi.copy()
@@ -71,6 +72,14 @@ def run_tc_records(prog, psi, blocks=None):
             Ar = np.stack([A.real, A.imag], -1).reshape(A.shape[:-1] + (64,))
             Y = Ar @ Bm
             Y = Y[..., 0::2] + 1j * Y[..., 1::2]
+            fac = int(blk["fac"])
+            if fac >= 0:  # per-thread factor table, indexed by outside bits
+                p = np.zeros(len(tiles), dtype=np.int64)
+                for k in range(int(blk["nout"])):
+                    pos = int(blk["opos"][k])
+                    p |= ((tiles >> outside.index(pos)) & 1) << k
+                f = factors[fac + p[:, None] * 128 + r[None, :]]
+                Y = Y * f[None, :, :, None]
             f0, nd = int(blk["first_diag"]), int(blk["num_diag"])
             for dg in diags[f0:f0 + nd]:
                 idx = np.zeros((len(tiles), 128, 32), dtype=np.int64)
@@ -167,7 +176,7 @@ def test_tc_image_split_is_exact_integer_plus_residual():
     a = rng.normal(size=(32, 32)) + 1j * rng.normal(size=(32, 32))
     U, _ = np.linalg.qr(a)
     img = tcplan.block_image(U)
-    bh = img[:4096].astype(np.float64)
+    bh = img[tcplan._IMG_IDX[64:]].astype(np.float64)
     assert np.all(bh == np.rint(bh)) and np.abs(bh).max() <= 1024
     # column L1 norms of the real form stay within the exactness bound
     B = tcplan.image_matrix(img)
