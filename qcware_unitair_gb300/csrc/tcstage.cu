@@ -128,16 +128,18 @@ __device__ __forceinline__ uint32_t tc_smem(const void* p) {
 }
 
 // Wait for phase `parity` of an mbarrier, for at most about 2^31 cycles.
+// try_wait suspends the thread until the phase completes or the hinted
+// time (1 ms) passes, so a waiting warp takes no issue slots.
 __device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity) {
   const long long t0 = clock64();
   while (true) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(bar), "r"(parity)
+        : "r"(bar), "r"(parity), "r"(1000000u)
         : "memory");
     if (ok) return true;
     if (clock64() - t0 > (1ll << 31)) return false;
