@@ -875,6 +875,84 @@ def run_gpu(args, ws, rank, local):
     mats_host = [torch.from_numpy(g.matrix()).to(torch.complex64)
                  for g in gates]
     mats = [m.to(dev) for m in mats_host]
+    # ---- e2e through the public functional API, host buffers -----------
+    # Measured first, on device memory no earlier phase has fragmented:
+    # after the device-timed phases the 8 GiB copies ran 2-10x slower
+    # (the same copy alone: 41 ms at 211 GB/s).
+    # pinned buffers are placed from the GPU's local CPUs: pages pinned on
+    # a far NUMA node cut host-to-device bandwidth several-fold
+    cpus = _gpu_local_cpus(dev)
+    old_aff = os.sched_getaffinity(0)
+    try:
+        if cpus:
+            os.sched_setaffinity(0, cpus)
+    except OSError:
+        pass
+    try:
+        host_in = torch.zeros(N, dtype=torch.complex64, pin_memory=True)
+        host_in[0] = 1
+        host_out = torch.zeros(N, dtype=torch.complex64, pin_memory=True)
+        # the step's gate matrices as one pinned tensor per size (one copy
+        # each instead of a thousand small ones)
+        sizes = sorted({m.shape[-1] for m in mats_host})
+        stacked = {d: torch.stack([m for m in mats_host if m.shape[-1] == d])
+                   .pin_memory() for d in sizes}
+        slot = []
+        seen = {d: 0 for d in sizes}
+        for m in mats_host:
+            d = m.shape[-1]
+            slot.append((d, seen[d]))
+            seen[d] += 1
+    finally:
+        try:
+            os.sched_setaffinity(0, old_aff)
+        except OSError:
+            pass
+
+    def e2e_step(ev=None):
+        if ev is not None:
+            ev[0].record()
+        state = host_in.to(dev, non_blocking=True)
+        dmats = {d: t.to(dev, non_blocking=True) for d, t in stacked.items()}
+        ops = [dmats[d][i] for d, i in slot]
+        if ev is not None:
+            ev[1].record()
+        for g, m in zip(gates, ops):
+            state = ug.apply_operator(m, g.qubits, state)
+        if ev is not None:
+            ev[2].record()
+        host_out.copy_(state, non_blocking=True)
+        if ev is not None:
+            ev[3].record()
+        return state
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    e2e_steps = max(1, min(args.steps, 2))
+    gc.collect()
+    gc.disable()  # no collector pauses inside the timed host loop
+    e2e_ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)]
+              for _ in range(e2e_steps)]
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        e2e_step(e2e_ev[k])
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dev)
+    gc.enable()
+    # where an e2e step's time goes (CUDA events on the launching stream)
+    e2e_parts = {
+        name: round(statistics.mean(ev[i].elapsed_time(ev[i + 1])
+                                    for ev in e2e_ev), 2)
+        for i, name in enumerate(("h2d_ms", "gates_ms", "d2h_ms"))}
+    e2e_parts["wall_ms"] = round(1e3 * e2e_s / e2e_steps, 2)
+    e2e_value = bytes_per_gate * G * e2e_steps * ws / e2e_s / 1e9
+    h2d = N * 8 + sum(m.numel() * 8 for m in mats_host)
+    d2h = N * 8
+    # final state sanity: unit norm
+    drift = abs(float(np.sum(np.abs(host_out.numpy().astype(np.complex128))
+                             ** 2)) - 1.0)
+
     psi = torch.zeros(N, dtype=torch.complex64, device=dev)
     stream = torch.cuda.current_stream(dev)
 
@@ -974,83 +1052,6 @@ def run_gpu(args, ws, rank, local):
     reg_ms, _, reg_norm, _ = fused_run(prog_reg)
     del prog_reg
 
-    # ---- e2e through the public functional API, host buffers -----------
-    # pinned buffers are placed from the GPU's local CPUs: pages pinned on
-    # a far NUMA node cut host-to-device bandwidth several-fold
-    cpus = _gpu_local_cpus(dev)
-    old_aff = os.sched_getaffinity(0)
-    try:
-        if cpus:
-            os.sched_setaffinity(0, cpus)
-    except OSError:
-        pass
-    try:
-        host_in = torch.zeros(N, dtype=torch.complex64, pin_memory=True)
-        host_in[0] = 1
-        host_out = torch.zeros(N, dtype=torch.complex64, pin_memory=True)
-        # the step's gate matrices as one pinned tensor per size (one copy
-        # each instead of a thousand small ones)
-        sizes = sorted({m.shape[-1] for m in mats_host})
-        stacked = {d: torch.stack([m for m in mats_host if m.shape[-1] == d])
-                   .pin_memory() for d in sizes}
-        slot = []
-        seen = {d: 0 for d in sizes}
-        for m in mats_host:
-            d = m.shape[-1]
-            slot.append((d, seen[d]))
-            seen[d] += 1
-    finally:
-        try:
-            os.sched_setaffinity(0, old_aff)
-        except OSError:
-            pass
-    del psi
-    torch.cuda.empty_cache()
-
-    def e2e_step(ev=None):
-        if ev is not None:
-            ev[0].record()
-        state = host_in.to(dev, non_blocking=True)
-        dmats = {d: t.to(dev, non_blocking=True) for d, t in stacked.items()}
-        ops = [dmats[d][i] for d, i in slot]
-        if ev is not None:
-            ev[1].record()
-        for g, m in zip(gates, ops):
-            state = ug.apply_operator(m, g.qubits, state)
-        if ev is not None:
-            ev[2].record()
-        host_out.copy_(state, non_blocking=True)
-        if ev is not None:
-            ev[3].record()
-        return state
-
-    e2e_step()
-    torch.cuda.synchronize()
-    barrier()
-    e2e_steps = max(1, min(args.steps, 2))
-    gc.collect()
-    gc.disable()  # no collector pauses inside the timed host loop
-    e2e_ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)]
-              for _ in range(e2e_steps)]
-    t0 = time.perf_counter()
-    for k in range(e2e_steps):
-        e2e_step(e2e_ev[k])
-    torch.cuda.synchronize()
-    e2e_s = max_over_ranks(time.perf_counter() - t0, dev)
-    gc.enable()
-    # where an e2e step's time goes (CUDA events on the launching stream)
-    e2e_parts = {
-        name: round(statistics.mean(ev[i].elapsed_time(ev[i + 1])
-                                    for ev in e2e_ev), 2)
-        for i, name in enumerate(("h2d_ms", "gates_ms", "d2h_ms"))}
-    e2e_parts["wall_ms"] = round(1e3 * e2e_s / e2e_steps, 2)
-    e2e_value = bytes_per_gate * G * e2e_steps * ws / e2e_s / 1e9
-    h2d = N * 8 + sum(m.numel() * 8 for m in mats_host)
-    d2h = N * 8
-    # final state sanity: unit norm
-    drift = abs(float(np.sum(np.abs(host_out.numpy().astype(np.complex128))
-                             ** 2)) - 1.0)
-
     peak, peak_kind = peaks()
     achieved = bytes_per_gate / (gate_ms / 1e3) / 1e9
     result = {
@@ -1079,6 +1080,7 @@ def run_gpu(args, ws, rank, local):
                      "launch_ms_p50": round(statistics.median(per_launch_ms),
                                             4),
                      "launch_ms_max": round(max(per_launch_ms), 4)},
+        "e2e_step_parts": e2e_parts,
         "e2e": {"value": round(e2e_value, 1), "unit": "GB/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "api": "qcware_unitair_gb300.apply_operator (functional)",
