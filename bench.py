@@ -1048,6 +1048,18 @@ def run_gpu(args, ws, rank, local):
     prog = circ.compile(torch.complex64, dev)
     fused_ms, fused_launches, fused_norm, tc_stage_ms = fused_run(prog)
     stage_ms = fused_ms / prog.num_passes
+    # the same circuit with a renormalisation checkpoint every 16 passes
+    reset()
+    ra = torch.cuda.Event(enable_timing=True)
+    rb = torch.cuda.Event(enable_timing=True)
+    ra.record(stream)
+    prog.run(psi, inplace=True, renorm_every=16)
+    rb.record(stream)
+    torch.cuda.synchronize()
+    renorm = {"every_passes": 16, "ms_per_step": round(ra.elapsed_time(rb), 3),
+              "drift_removed": prog.renorm_drift(),
+              "final_norm_drift": abs(float(torch.linalg.vector_norm(
+                  psi.to(torch.complex128))) ** 2 - 1.0)}
     prog_reg = circ.compile(torch.complex64, dev, tensor_cores=False)
     reg_ms, _, reg_norm, _ = fused_run(prog_reg)
     del prog_reg
@@ -1106,6 +1118,8 @@ def run_gpu(args, ws, rank, local):
                                     if tc_stage_ms else None,
             "launches_per_step": fused_launches,
             "final_norm": fused_norm,
+            "final_norm_drift": abs(fused_norm ** 2 - 1.0),
+            "with_renorm_checkpoints": renorm,
             "register_stages_ms": round(reg_ms, 3),
             "speedup_vs_register_stages": round(reg_ms / fused_ms, 3),
             "register_stages_final_norm": reg_norm},

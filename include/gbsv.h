@@ -448,6 +448,19 @@ int gbsv_norm_squared(const void* state, int dtype, int64_t num_rows,
                       int64_t dim, void* out, int out_dtype, void* scratch,
                       size_t scratch_bytes, void* stream);
 
+/* Renormalisation checkpoint for deep circuits: measures every row's
+ * squared norm (FP64 accumulation, written to norms_out, device float64
+ * [num_rows]) and scales the row in place so its squared norm becomes
+ * target_norms[row] (device float64 [num_rows]; typically the norms the
+ * circuit started from, which a unitary circuit preserves).  Rounding in
+ * long gate sequences drifts the norm; the caller reads the drift from
+ * norms_out.  scratch as for gbsv_norm_squared.  Keeps the quantity
+ * unitair's norm_squared reports (src/unitair/states/innerprod.py:29-46)
+ * fixed; unitair itself has no such step. */
+int gbsv_renormalize(void* state, int dtype, int64_t num_rows, int64_t dim,
+                     const void* target_norms, void* norms_out, void* scratch,
+                     size_t scratch_bytes, void* stream);
+
 /* gbsv_norm_squared for callers that cannot allocate device memory: a host
  * program that reaches the library through a thin FFI and holds only
  * buffers another runtime gave it has no allocator to call, and a

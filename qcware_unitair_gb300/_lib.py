@@ -113,6 +113,7 @@ SIGNATURES = {
     "gbsv_reduce_scratch_bytes": (_SZ, [_I64, _I64]),
     "gbsv_norm_squared": (_I, [_P, _I, _I64, _I64, _P, _I, _P, _SZ, _P]),
     "gbsv_norm_squared_noalloc": (_I, [_P, _I, _I64, _I64, _P, _I, _P]),
+    "gbsv_renormalize": (_I, [_P, _I, _I64, _I64, _P, _P, _P, _SZ, _P]),
     "gbsv_abs_squared": (_I, [_P, _I, _I64, _P, _P]),
     "gbsv_inner_product": (_I, [_P, _P, _I, _BC, _I64, _I64, _I64, _P, _I,
                                 _P, _SZ, _P]),

@@ -405,6 +405,32 @@ static int check_scratch(const Plan& p, int64_t rows, int complex_parts,
   return GBSV_OK;
 }
 
+
+// ---- renormalisation checkpoint ---------------------------------------
+// psi[row] *= sqrt(target[row] / norm[row]); a block covers `per_block`
+// amplitudes of one row and computes the row's factor once (FP64).
+template <typename R>
+__global__ void __launch_bounds__(RED_THREADS)
+    rescale_kernel(Cx<R>* psi, int64_t dim, int64_t per_block,
+                   const double* target, const double* norm) {
+  const int64_t blocks_per_row = dim / per_block;
+  const int64_t row = blockIdx.x / blocks_per_row;
+  const int64_t lo = row * dim + (blockIdx.x % blocks_per_row) * per_block;
+  __shared__ R fac;
+  if (threadIdx.x == 0) {
+    const double n = norm[row];
+    fac = (R)(n > 0.0 ? sqrt(target[row] / n) : 1.0);
+  }
+  __syncthreads();
+  const R f = fac;
+  for (int64_t i = lo + threadIdx.x; i < lo + per_block; i += RED_THREADS) {
+    Cx<R> v = psi[i];
+    v.x *= f;
+    v.y *= f;
+    psi[i] = v;
+  }
+}
+
 static int finalize(const Plan& p, double* partial, int complex_parts,
                     int64_t rows, void* out, int out_dtype, cudaStream_t st) {
   if (p.parts == 1) return GBSV_OK;
@@ -463,6 +489,41 @@ extern "C" int gbsv_norm_squared(const void* state, int dtype,
   rc = after_launch("norm2_kernel");
   if (rc) return rc;
   return finalize(p, partial, 0, num_rows, out, out_dtype, st);
+}
+
+extern "C" int gbsv_renormalize(void* state, int dtype, int64_t num_rows,
+                                int64_t dim, const void* target_norms,
+                                void* norms_out, void* scratch,
+                                size_t scratch_bytes, void* stream) {
+  if (dtype != GBSV_C64 && dtype != GBSV_C128)
+    return set_error(GBSV_ERR_INVALID_ARG, "state must be complex");
+  if (num_rows < 0 || dim < 0)
+    return set_error(GBSV_ERR_INVALID_ARG, "negative size");
+  if (num_rows == 0 || dim == 0) return GBSV_OK;
+  if (dim & (dim - 1))
+    return set_error(GBSV_ERR_INVALID_ARG, "dim must be a power of two");
+  if (!state || !target_norms || !norms_out)
+    return set_error(GBSV_ERR_INVALID_ARG, "null pointer");
+  int rc = gbsv_norm_squared(state, dtype, num_rows, dim, norms_out,
+                             GBSV_F64, scratch, scratch_bytes, stream);
+  if (rc) return rc;
+  const int64_t per_block = dim < 8192 ? dim : 8192;
+  const uint64_t blocks = (uint64_t)num_rows * (uint64_t)(dim / per_block);
+  if (blocks > 0x7fffffffull)
+    return set_error(GBSV_ERR_UNSUPPORTED, "too many rows (%lld)",
+                     (long long)num_rows);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (dtype == GBSV_C64)
+    rescale_kernel<float><<<(unsigned)blocks, RED_THREADS, 0, st>>>(
+        static_cast<float2*>(state), dim, per_block,
+        static_cast<const double*>(target_norms),
+        static_cast<const double*>(norms_out));
+  else
+    rescale_kernel<double><<<(unsigned)blocks, RED_THREADS, 0, st>>>(
+        static_cast<double2*>(state), dim, per_block,
+        static_cast<const double*>(target_norms),
+        static_cast<const double*>(norms_out));
+  return after_launch("rescale_kernel");
 }
 
 extern "C" int gbsv_abs_squared(const void* state, int dtype, int64_t count,

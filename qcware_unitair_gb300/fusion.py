@@ -733,9 +733,17 @@ class Program:
         return len(self.ops)
 
     # -- running ---------------------------------------------------------
-    def run(self, state: torch.Tensor, inplace: bool = False) -> torch.Tensor:
+    def run(self, state: torch.Tensor, inplace: bool = False,
+            renorm_every: Optional[int] = None) -> torch.Tensor:
         """Apply the program to ``state`` (*batch, 2^n); a per-state gate
-        batch must equal the flattened state batch."""
+        batch must equal the flattened state batch.
+
+        ``renorm_every=K`` adds a renormalisation checkpoint after every K
+        passes (gbsv_renormalize): each state is rescaled to the squared
+        norm it started with, measured in FP64 before the first pass.  A
+        unitary circuit preserves the norm; rounding over thousands of gates
+        drifts it.  ``renorm_drift()`` reports the largest relative drift
+        the checkpoints removed."""
         _core.require_cuda(state)
         if state.dtype != self.dtype:
             raise RuntimeError(f"program compiled for {self.dtype}, state is "
@@ -762,10 +770,35 @@ class Program:
         cur = src
         if not self.ops and cur is not out:
             out.copy_(cur)
-        for op in self.ops:
+        self._renorm = []
+        if renorm_every:
+            from . import states as S
+            target = S.norm_squared_fp64(src.reshape(B, N))
+            nbytes = int(L.gbsv_reduce_scratch_bytes(B, N))
+            scratch = torch.empty(max(nbytes, 16), dtype=torch.uint8,
+                                  device=state.device)
+        for i, op in enumerate(self.ops):
             self._run_op(op, cur, out, B, N, L, stream)
             cur = out
+            if (renorm_every and (i + 1) % int(renorm_every) == 0
+                    and i + 1 < len(self.ops)):
+                norms = torch.empty(B, dtype=torch.float64,
+                                    device=state.device)
+                rc = L.gbsv_renormalize(out.data_ptr(), self.code, B, N,
+                                        target.data_ptr(), norms.data_ptr(),
+                                        scratch.data_ptr(), nbytes, stream)
+                _lib.check(rc, "renormalize")
+                self._renorm.append((norms, target))
         return out
+
+    def renorm_drift(self) -> float:
+        """Largest |norm^2 / target - 1| seen at the last run's
+        checkpoints (0 without checkpoints); synchronizes."""
+        worst = 0.0
+        for norms, target in getattr(self, "_renorm", []):
+            d = (norms / target.clamp_min(1e-300) - 1).abs().max()
+            worst = max(worst, float(d))
+        return worst
 
     def run_op(self, op, state: torch.Tensor) -> None:
         """One pass of the program (an entry of ``ops``), in place on a
