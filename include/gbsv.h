@@ -177,6 +177,33 @@ int gbsv_run_stage_layouts(const void* state_in, void* state_out, int dtype,
                            const void* layouts, int num_layouts,
                            const void* pool, void* stream);
 
+/* One register stage of a program, for gbsv_run_stages_multi (host
+ * array).  gates is the program's record array and layouts this stage's
+ * first layout record (device); tile_positions as for gbsv_run_stage. */
+typedef struct gbsv_multi_stage {
+  const void* state_in;
+  void* state_out;
+  const void* gates;
+  const void* layouts;
+  const void* pool;
+  int64_t num_states;
+  int64_t in_stride;
+  int32_t num_layouts;
+  int32_t contiguous_qubits;
+  int32_t tile_positions[16];
+} gbsv_multi_stage_t;
+
+/* gbsv_run_stage_layouts for many programs at once: stage i of the host
+ * array runs on its own states, all num_stages in one launch (batches of
+ * 48), the CTAs shared in proportion to each stage's tiles.  Every stage
+ * has num_qubits qubits and tile_qubits tile bits.  The serving loop
+ * launches the r-th stage of every admitted circuit of one size together,
+ * so small states fill the GPU.  No counterpart in unitair, which applies
+ * one operator to one batch at a time. */
+int gbsv_run_stages_multi(int dtype, int num_qubits, int tile_qubits,
+                          const gbsv_multi_stage_t* stages, int num_stages,
+                          void* stream);
+
 /* Many circuits in one launch: CTA i runs gates[gate_first[i] ..
  * gate_first[i] + gate_count[i]) (records as for gbsv_run_stage with the
  * whole state as the tile, i.e. tile bit b = amplitude-index bit b) on the

@@ -18,8 +18,13 @@ the GPU:
               complex64) are packed, whatever their circuits, into ONE
               multi-program launch per qubit count (gbsv_run_programs: one
               CTA per state, each running its own gate list).
-  streams     larger requests run as fused programs on a pool of CUDA
-              streams, so several requests' kernels overlap on the device.
+  batching    larger requests admitted together with the same qubit count
+              run as fused programs whose stages go out in rounds: round
+              r launches stage r of every one of them in ONE launch
+              (gbsv_run_stages_multi), so small states fill the GPU.
+  streams     the rest (gradient requests, a lone request of its size) run
+              as fused programs on a pool of CUDA streams, so several
+              requests' kernels overlap on the device.
   completion  CUDA events are polled; finished requests return norms and
               <Z_0> (FP64 reductions) and free their memory for the next
               admissions.
@@ -31,6 +36,7 @@ request with arrival, admission and completion times.
 from __future__ import annotations
 
 import collections
+import ctypes
 import dataclasses
 import math
 import time
@@ -322,6 +328,61 @@ class Server:
             ev.record(stream)
         return (ev, req, psi, o, grads, prog)
 
+    def _launch_large_batch(self, reqs):
+        """Requests with one qubit count (no gradients): their programs'
+        stages in rounds, one multi-program launch per round."""
+        n = reqs[0].num_qubits
+        stream = self._stream()
+        N = 2 ** n
+        L = _lib.load()
+        with torch.cuda.stream(stream):
+            items = []
+            for req in reqs:
+                psi = _init_states(req, self.device)
+                prog = Program.from_gate_list(req.gates, n, torch.complex64,
+                                              self.device)
+                items.append((req, psi, prog))
+        solo = [it for it in items
+                if any(op[0] != "layouts" for op in it[2].ops)
+                or it[2].m != items[0][2].m]
+        batch = [it for it in items if it not in solo]
+        out = []
+        with torch.cuda.stream(stream):
+            rounds = max((len(p.ops) for _, _, p in batch), default=0)
+            for r in range(rounds):
+                live = [it for it in batch if len(it[2].ops) > r]
+                descs = (_lib.MultiStage * len(live))()
+                for d, (req, psi, prog) in zip(descs, live):
+                    _, c, positions, first, count = prog.ops[r]
+                    d.state_in = d.state_out = psi.data_ptr()
+                    d.gates = prog.gate_records.data_ptr()
+                    d.layouts = prog.layout_records.data_ptr() + first * 32
+                    d.pool = prog.pool.data_ptr()
+                    d.num_states = req.num_states
+                    d.in_stride = N
+                    d.num_layouts = count
+                    d.contiguous_qubits = c
+                    for j in range(prog.m):
+                        d.tile_positions[j] = positions[j]
+                rc = L.gbsv_run_stages_multi(_lib.C64, n, live[0][2].m,
+                                             ctypes.cast(descs,
+                                                         ctypes.c_void_p),
+                                             len(live), stream.cuda_stream)
+                _lib.check(rc, "run_stages_multi")
+                for req, psi, prog in live:
+                    if len(prog.ops) == r + 1:  # this request is done
+                        o = _outputs(psi, n)
+                        ev = torch.cuda.Event()
+                        ev.record(stream)
+                        out.append((ev, req, psi, o, None, prog))
+            for req, psi, prog in solo:
+                prog.run(psi, inplace=True)
+                o = _outputs(psi, n)
+                ev = torch.cuda.Event()
+                ev.record(stream)
+                out.append((ev, req, psi, o, None, prog))
+        return out
+
     # -- the loop ---------------------------------------------------------
     def serve(self, trace: Sequence[Request]) -> List[Result]:
         """Replay the trace against the wall clock; one Result per
@@ -368,8 +429,17 @@ class Server:
                 by_n[req.num_qubits].append(req)
             for reqs in by_n.values():
                 inflight.extend(self._launch_small(reqs))
+            big_n = collections.defaultdict(list)
             for req in large:
-                inflight.append(self._launch_large(req))
+                if req.want_grad:
+                    inflight.append(self._launch_large(req))
+                else:
+                    big_n[req.num_qubits].append(req)
+            for reqs in big_n.values():
+                if len(reqs) == 1:
+                    inflight.append(self._launch_large(reqs[0]))
+                else:
+                    inflight.extend(self._launch_large_batch(reqs))
             # completion
             still = []
             for item in inflight:

@@ -89,3 +89,29 @@ def test_oversized_requests_split_by_state_blocks():
         if req.want_grad:
             assert np.abs(a.grads - b.grads).max() <= 1e-6 * max(
                 1.0, np.abs(a.grads).max())
+
+
+def test_same_size_requests_batched_in_rounds(oracle):
+    """Requests above the one-tile size that arrive together with the same
+    qubit count run their stages in shared launches (gbsv_run_stages_multi);
+    each result matches the request served alone and the oracle."""
+    trace = make_trace(12, rate=1e6, seed=8, qubits=(15, 16),
+                       depth=(30, 200), batch=(1, 4), grad_fraction=0.0)
+    server = Server(DEV, keep_states=True)
+    calls = []
+    orig = server._launch_large_batch
+
+    def spy(reqs):
+        calls.append(len(reqs))
+        return orig(reqs)
+    server._launch_large_batch = spy
+    mixed = server.serve(trace)
+    assert calls and max(calls) >= 2
+    for req, res in zip(trace, mixed):
+        alone = Server(DEV, keep_states=True).serve([req])[0]
+        assert np.abs(res.final.cpu().numpy() -
+                      alone.final.cpu().numpy()).max() <= 1e-5
+        psi0 = _init_states(req, DEV).cpu().numpy().astype(np.complex128)
+        ref = oracle.run_circuit([(g.matrix(), g.qubits) for g in req.gates],
+                                 psi0)
+        assert np.abs(res.final.cpu().numpy() - ref).max() <= 1e-5
