@@ -472,36 +472,54 @@ class Server:
 
 
 def serve_plain(trace: Sequence[Request], device="cuda",
-                keep_states: bool = False) -> List[Result]:
-    """Baseline: FIFO, one request at a time, one kernel per gate."""
+                keep_states: bool = False,
+                wall_cap_s: Optional[float] = None,
+                budget_bytes: float = 160e9) -> List[Result]:
+    """Baseline: FIFO, one request at a time, one kernel per gate.  A
+    request larger than the HBM budget runs as the server's parts of whole
+    state blocks, one after another.  With ``wall_cap_s`` no request starts
+    after that many seconds; only the finished requests are returned."""
     dev = torch.device(device)
     out = []
     t0 = time.perf_counter()
-    for req in sorted(trace, key=lambda r: r.arrival):
+    for whole in sorted(trace, key=lambda r: r.arrival):
         now = time.perf_counter() - t0
-        if now < req.arrival:
-            time.sleep(req.arrival - now)
-        admitted = time.perf_counter() - t0
-        psi = _init_states(req, dev)
-        grads = None
-        if req.want_grad:
-            grads = _run_grad(req, psi, fuse=False)
-        # all of the request's gate matrices in one transfer, then one
-        # kernel per gate
-        mats = [torch.from_numpy(g.matrix()) for g in req.gates]
-        by_size = {}
-        for d in (2, 4):
-            sel = [m for m in mats if m.shape[-1] == d]
-            if sel:
-                by_size[d] = iter(torch.stack(sel).to(torch.complex64)
-                                  .pin_memory().to(dev, non_blocking=True))
-        for g, m in zip(req.gates, mats):
-            simulation.apply_operator_(next(by_size[m.shape[-1]]), g.qubits,
-                                       psi)
-        norms, z0 = _outputs(psi, req.num_qubits)
-        res = Result(req.rid, norms.cpu().numpy(), z0.cpu().numpy(),
-                     grads.cpu().numpy() if grads is not None else None,
-                     req.arrival, admitted, time.perf_counter() - t0,
-                     psi if keep_states else None)
-        out.append(res)
+        if wall_cap_s is not None and now > wall_cap_s:
+            break
+        if now < whole.arrival:
+            time.sleep(whole.arrival - now)
+        pieces = []
+        for req in whole.split(budget_bytes):
+            pieces.append((req.state_offset,
+                           _plain_one(req, dev, t0, keep_states)))
+        out.append(pieces[0][1] if len(pieces) == 1 else
+                   _merge_parts(pieces))
     return sorted(out, key=lambda r: r.rid)
+
+
+def _plain_one(req: Request, dev, t0: float, keep_states: bool) -> Result:
+    """One request (or part) on the plain per-gate path."""
+    admitted = time.perf_counter() - t0
+    psi = _init_states(req, dev)
+    grads = None
+    if req.want_grad:
+        grads = _run_grad(req, psi, fuse=False)
+    # all of the request's gate matrices in one transfer, then one
+    # kernel per gate
+    mats = [torch.from_numpy(g.matrix()) for g in req.gates]
+    by_size = {}
+    for d in (2, 4):
+        sel = [m for m in mats if m.shape[-1] == d]
+        if sel:
+            by_size[d] = iter(torch.stack(sel).to(torch.complex64)
+                              .pin_memory().to(dev, non_blocking=True))
+    for g, m in zip(req.gates, mats):
+        simulation.apply_operator_(next(by_size[m.shape[-1]]), g.qubits,
+                                   psi)
+    norms, z0 = _outputs(psi, req.num_qubits)
+    res = Result(req.rid, norms.cpu().numpy(), z0.cpu().numpy(),
+                 grads.cpu().numpy() if grads is not None else None,
+                 req.arrival, admitted, time.perf_counter() - t0,
+                 psi if keep_states else None)
+    del psi
+    return res
