@@ -1196,6 +1196,43 @@ def run_gpu(args, ws, rank, local):
         dist.destroy_process_group()
 
 
+def unitair_sample(num_qubits: int, seed: int, budget_s: float = 10.0):
+    """unitair's own torch CPU path (apply_operator, operations.py:45-148),
+    installed under baseline/_ref, on every host thread: the canonical
+    circuit's first gates on a num_qubits complex64 state from |0...0>
+    until budget_s passes, as algorithmic GB/s (2 x 8 B x 2^n per gate)."""
+    ref = REPO / "baseline" / "_ref"
+    if not (ref / "unitair").is_dir():
+        return {"unavailable": "baseline/_ref has no unitair install"}
+    sys.path.insert(0, str(ref))
+    try:
+        import torch
+        import unitair.simulation as usim
+    except ImportError as e:
+        return {"unavailable": f"unitair import failed: {e}"}
+    from qcware_unitair_gb300.circuits import random_circuit
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    gates = random_circuit(num_qubits, 1000, seed=seed)
+    psi = torch.zeros(2 ** num_qubits, dtype=torch.complex64)
+    psi[0] = 1
+    mats = [torch.from_numpy(g.matrix()).to(torch.complex64) for g in gates]
+    psi = usim.apply_operator(mats[0], list(gates[0].qubits), psi)  # warm
+    done, t0 = 0, time.perf_counter()
+    for g, m in zip(gates, mats):
+        psi = usim.apply_operator(m, list(g.qubits), psi)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": round(done * 2 * 8 * 2 ** num_qubits / dt / 1e9, 3),
+            "unit": "GB/s", "qubits": num_qubits, "threads": threads,
+            "gates_timed": done, "s_per_gate": round(dt / done, 4),
+            "api": "unitair.simulation.apply_operator (torch CPU)",
+            "sample": f"first {done} gates of the {num_qubits}-qubit "
+                      f"canonical circuit, {dt:.1f} s"}
+
+
 def run_reference(args, ws, rank):
     """Reference arm: the oracle's C port of the reference path (complex64
     arithmetic, OpenMP over all host threads); each step is a bounded sample
@@ -1229,6 +1266,9 @@ def run_reference(args, ws, rank):
                          "sample": vals[0]["sample"]},
         "e2e": {"value": round(v, 3), "unit": "GB/s",
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        # unitair itself, beside the port (a 30-qubit state is out of its
+        # reach in a bounded run: about three 8 GiB copies per gate)
+        "unitair": unitair_sample(24, args.seed),
     }
     print(json.dumps(result), flush=True)
 
