@@ -19,6 +19,7 @@ from .measurement import measure, MeasurementHistogram  # noqa
 from .fusion import Circuit, Program  # noqa
 from .initializations import (unit_vector, uniform_superposition,  # noqa
                               rand_state)
+from . import library  # noqa: F401  (torch.ops.gbsv.*)
 
 VECTOR_LAYOUT = StateLayout.VECTOR
 TENSOR_LAYOUT = StateLayout.TENSOR
