@@ -24,11 +24,15 @@ namespace gbsv {
 // that both the reads and the writes are runs of 2^c contiguous amplitudes.
 // Tile bits T (input positions): bits 0..c-1 (contiguous reads) plus the
 // input bits that land on output bits 0..c-1 (contiguous writes), topped up
-// with the lowest other bits to at least 11 (2048 amplitudes, 8 per
-// thread, so the per-tile index work is amortised).  A CTA reads a tile in input
+// with the lowest other bits to 12 for complex64 (c = 6: both sides move
+// runs of at least 512 bytes, which a full qubit reversal needs to reach
+// the copy rate) or 11 for complex128 (c = 5), 8 amplitudes per thread so
+// the per-tile index work is amortised.  A CTA reads a tile in input
 // order into shared memory and writes it back in output order; the other
 // bits pick the tile and move as a block.
-constexpr int PERM_MAX_TB = 11;
+constexpr int PERM_MAX_TB = 12;
+template <typename R>
+constexpr int perm_tile_bits() { return sizeof(R) == 4 ? 12 : 11; }
 
 struct PermArgs {
   int n, tb;
@@ -40,20 +44,27 @@ struct PermArgs {
   uint64_t tiles_per_state, total_tiles;
 };
 
+// Shared-memory swizzle of tile element l: every group of higher bits is
+// XOR-folded onto the bank bits (4 for 8-byte elements, 3 for 16-byte), so
+// lanes that walk any single high tile bit still hit distinct banks, on
+// the read side and on the write side of the transpose.
 template <typename R>
 __device__ __forceinline__ int perm_swz(int l) {
-  return sizeof(R) == 4 ? (l ^ ((l >> 4) & 15)) : (l ^ ((l >> 3) & 7));
+  return sizeof(R) == 4 ? (l ^ (((l >> 4) ^ (l >> 8)) & 15))
+                        : (l ^ (((l >> 3) ^ (l >> 6) ^ (l >> 9)) & 7));
 }
 
-template <typename R>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2)
+// O: the offset type of tile elements within a state (uint32_t up to 32
+// qubits, which keeps the per-thread tables in registers)
+template <typename R, typename O>
+__global__ void __launch_bounds__(sizeof(R) == 4 ? 512 : 256, 2)
     permute_kernel(const Cx<R>* in, Cx<R>* out, PermArgs a) {
   using C = Cx<R>;
-  __shared__ C S[1 << PERM_MAX_TB];
+  __shared__ C S[1 << perm_tile_bits<R>()];
   const int M = 1 << a.tb, T = blockDim.x, tid = threadIdx.x;
   const int K = M / T;  // elements per thread per tile, <= 8
   // per-thread offsets of its K tile elements, read and write side
-  uint64_t roff[8], woff[8];
+  O roff[8], woff[8];
   int rl[8], wsm[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
@@ -64,12 +75,12 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2)
   for (int k = 0; k < 8; ++k) {
     if (k >= K) break;
     const int l = tid + k * T;
-    uint64_t ro = 0, wo = 0;
+    O ro = 0, wo = 0;
     int ls = 0;
     for (int j = 0; j < a.tb; ++j) {
       if ((l >> j) & 1) {
-        ro |= uint64_t(1) << a.tin[j];
-        wo |= uint64_t(1) << a.wp[j];
+        ro |= O(1) << a.tin[j];
+        wo |= O(1) << a.wp[j];
         ls |= 1 << a.wl[j];
       }
     }
@@ -542,10 +553,12 @@ extern "C" int gbsv_permute_qubits(const void* in, void* out, int dtype,
   }
   PermArgs a{};
   a.n = n;
-  const int c = n < 5 ? n : 5;
+  const int tbmax = dtype == GBSV_C64 ? 12 : 11;
+  const int cw = dtype == GBSV_C64 ? 6 : 5;
+  const int c = n < cw ? n : cw;
   uint64_t tmask = (uint64_t(1) << c) - 1;
   for (int p = 0; p < c; ++p) tmask |= uint64_t(1) << src_pos[p];
-  for (int b = 0; b < n && __builtin_popcountll(tmask) < PERM_MAX_TB; ++b)
+  for (int b = 0; b < n && __builtin_popcountll(tmask) < tbmax; ++b)
     tmask |= uint64_t(1) << b;
   a.tb = __builtin_popcountll(tmask);
   // tile-local order: input bits 0..c-1 first, then the rest ascending
@@ -571,16 +584,25 @@ extern "C" int gbsv_permute_qubits(const void* in, void* out, int dtype,
     }
   a.tiles_per_state = uint64_t(1) << (n - a.tb);
   a.total_tiles = (uint64_t)num_states * a.tiles_per_state;
-  const int threads = (1 << a.tb) < 256 ? (1 << a.tb) : 256;  // K <= 8
+  // 8 elements per thread (tiles of 2^12 complex64 / 2^11 complex128: 512 /
+  // 256 threads, the kernel's launch bound); a warp or less for tiny states
+  const int M = 1 << a.tb;
+  const int threads = M >= 256 ? M / 8 : (M < 32 ? M : 32);
   uint64_t grid = a.total_tiles;
-  const uint64_t cap = (uint64_t)sm_count() * 8;
+  const uint64_t cap = (uint64_t)sm_count() * 4;
   if (grid > cap) grid = cap;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (dtype == GBSV_C64)
-    permute_kernel<float><<<(unsigned)grid, threads, 0, st>>>(
+  if (dtype == GBSV_C64 && n <= 32)
+    permute_kernel<float, uint32_t><<<(unsigned)grid, threads, 0, st>>>(
         static_cast<const float2*>(in), static_cast<float2*>(out), a);
+  else if (dtype == GBSV_C64)
+    permute_kernel<float, uint64_t><<<(unsigned)grid, threads, 0, st>>>(
+        static_cast<const float2*>(in), static_cast<float2*>(out), a);
+  else if (n <= 32)
+    permute_kernel<double, uint32_t><<<(unsigned)grid, threads, 0, st>>>(
+        static_cast<const double2*>(in), static_cast<double2*>(out), a);
   else
-    permute_kernel<double><<<(unsigned)grid, threads, 0, st>>>(
+    permute_kernel<double, uint64_t><<<(unsigned)grid, threads, 0, st>>>(
         static_cast<const double2*>(in), static_cast<double2*>(out), a);
   return after_launch("permute_kernel");
 }

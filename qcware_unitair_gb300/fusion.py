@@ -518,16 +518,19 @@ class Program:
                     raise ValueError("per-state gates must share one batch "
                                      "size")
                 self.batch = b
-        # tensor-core stages: complex64, shared matrices, 12-bit tiles
+        # tensor-core stages: complex64, shared matrices held on the host
+        # (their block products are formed there; matrices already on the
+        # device stay on the register path, which needs no host copy)
         tc_ok = (fuse and dtype == torch.complex64 and n >= 12
-                 and self.batch is None and tile_qubits in (None, 12))
+                 and self.batch is None and tile_qubits in (None, 12)
+                 and not any(g.matrix.is_cuda for g in circuit.gates))
         if tensor_cores is None:
             tensor_cores = tc_ok and layouts
         if tensor_cores:
             if not tc_ok:
                 raise ValueError("tensor-core stages need complex64, at "
-                                 "least 12 qubits, shared gate matrices and "
-                                 "12 tile qubits")
+                                 "least 12 qubits, shared gate matrices on "
+                                 "the host and 12 tile qubits")
             from . import tcplan
             self.m = tcplan.TC_M
             self._build_tc(tcplan.plan_tc(circuit.gates, n, self.c_min))
