@@ -840,20 +840,41 @@ def wl_serve(num: int = 300) -> float:
     return res["circuits_per_s"]
 
 
-def wl_kinds(n: int = 28) -> None:
+def wl_kinds(n: int = 28, mode: str = "pairs") -> None:
+    """Each complex128 gate kind on an n-qubit state, in the given
+    arithmetic mode ("pairs" or "fp64"); 10 timed launches after 2."""
+    import numpy as np
     import torch
     import qcware_unitair_gb300 as ug
     from qcware_unitair_gb300.circuits import gate_matrix
+    ug.set_complex128_arithmetic(mode)
     dev = torch.device("cuda")
     psi = torch.randn(2 ** n, dtype=torch.complex128, device=dev)
     psi /= psi.abs().pow(2).sum().sqrt()
+    rng = np.random.default_rng(0)
+
+    def unitary(k):
+        q, _ = np.linalg.qr(rng.normal(size=(2 ** k, 2 ** k)) +
+                            1j * rng.normal(size=(2 ** k, 2 ** k)))
+        return q
+
+    cry = np.eye(4, dtype=np.complex128)
+    cry[2:, 2:] = gate_matrix("RY", 0.7)
     cases = [("X", [5]), ("H", [5]), ("RY", [5]), ("RX", [5]), ("RZ", [5]),
-             ("T", [5]), ("Z", [5]), ("Y", [5]), ("CNOT", [3, 20]),
-             ("CZ", [3, 20]), ("SWAP", [3, 20]), ("X", [n - 1]),
+             ("T", [5]), ("Z", [5]), ("Y", [5]), ("S", [5]), ("U2", [5]),
+             ("CNOT", [3, 20]), ("CZ", [3, 20]), ("SWAP", [3, 20]),
+             ("CRY", [3, 20]), ("U4", [3, 20]), ("X", [n - 1]),
              ("RX", [n - 1]), ("CNOT", [n - 2, n - 1])]
     for name, q in cases:
-        theta = 0.7 if name.startswith("R") else None
-        m = torch.from_numpy(gate_matrix(name, theta)).to(dev)
+        if name == "U2":
+            mat = unitary(1)
+        elif name == "U4":
+            mat = unitary(2)
+        elif name == "CRY":
+            mat = cry
+        else:
+            mat = gate_matrix(name, 0.7 if name.startswith("R") else None)
+        m = torch.from_numpy(mat).to(dev)
         for _ in range(2):
             ug.apply_operator_(m, q, psi)
         torch.cuda.synchronize()
@@ -865,8 +886,9 @@ def wl_kinds(n: int = 28) -> None:
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / 10
-        print(f"kinds n={n} {name} {q}: {ms:.3f} ms "
+        print(f"kinds n={n} {mode} {name} {q}: {ms:.3f} ms "
               f"{2 * 16 * 2 ** n / ms / 1e6:.0f} GB/s")
+
 
 def run_workload(argv):
     import torch  # noqa: F401  (CUDA initialised before the workload)
@@ -884,7 +906,8 @@ def run_workload(argv):
     elif what == "serve":
         wl_serve(*(int(a) for a in args))
     elif what == "kinds":
-        wl_kinds(*(int(a) for a in args))
+        wl_kinds(int(args[0]) if args else 28,
+                 args[1] if len(args) > 1 else "pairs")
     else:
         raise SystemExit(f"unknown workload {what}")
 

@@ -77,6 +77,21 @@ const char* gbsv_last_error(void);
 /* Number of kernels this library has launched in this process. */
 uint64_t gbsv_launch_count(void);
 
+/* ---- complex128 arithmetic --------------------------------------------- */
+#define GBSV_C128_PAIRS 0  /* double-float pairs on the FP32 pipe (default) */
+#define GBSV_C128_FP64 1   /* native FP64 */
+
+/* Process-wide choice of the complex128 gate arithmetic.  GB300 issues FP64
+ * at about 1/64 of its FP32 rate, so by default the complex128 gate kernels
+ * (gbsv_apply_operator with one operator shared by every state) compute in
+ * pairs of floats: about 47 significant bits, a relative error of a few
+ * 2^-47 per gate with no bias; amplitudes and entries outside [2^-40, 2^60]
+ * still take FP64.  GBSV_C128_FP64 restores FP64 throughout.  No
+ * counterpart in unitair (its complex128 path is torch's CPU FP64).
+ * Returns GBSV_ERR_INVALID_ARG for an unknown mode. */
+int gbsv_set_c128_arith(int mode);
+int gbsv_get_c128_arith(void);
+
 /* ---- gate application ------------------------------------------------- */
 
 /* Apply a dense k-qubit operator (0 <= k <= GBSV_MAX_DENSE_QUBITS) to the

@@ -20,6 +20,8 @@ from .fusion import Circuit, Program  # noqa
 from .initializations import (unit_vector, uniform_superposition,  # noqa
                               rand_state)
 from . import library  # noqa: F401  (torch.ops.gbsv.*)
+from ._lib import (set_complex128_arithmetic,  # noqa: F401
+                   complex128_arithmetic)
 
 VECTOR_LAYOUT = StateLayout.VECTOR
 TENSOR_LAYOUT = StateLayout.TENSOR

@@ -82,6 +82,8 @@ SIGNATURES = {
     "gbsv_status_string": (ctypes.c_char_p, [_I]),
     "gbsv_last_error": (ctypes.c_char_p, []),
     "gbsv_launch_count": (ctypes.c_uint64, []),
+    "gbsv_set_c128_arith": (_I, [_I]),
+    "gbsv_get_c128_arith": (_I, []),
     "gbsv_apply_operator": (_I, [_P, _P, _I, _I, _I64, _I64, _P, _I64,
                                  ctypes.POINTER(_I32), _I, _P]),
     "gbsv_apply_all_qubits": (_I, [_P, _P, _I, _I, _I64, _I64, _P, _I64,
@@ -172,6 +174,26 @@ def check(status: int, what: str) -> None:
 
 def launch_count() -> int:
     return int(load().gbsv_launch_count())
+
+
+C128_ARITH = {"pairs": 0, "fp64": 1}
+
+
+def set_complex128_arithmetic(mode: str) -> str:
+    """Select the complex128 gate arithmetic for this process: "pairs"
+    (double-float pairs on the FP32 pipe, about 47 bits, the default) or
+    "fp64" (native FP64).  Returns the previous mode."""
+    if mode not in C128_ARITH:
+        raise ValueError(f"complex128 arithmetic must be one of "
+                         f"{sorted(C128_ARITH)}, not {mode!r}")
+    prev = complex128_arithmetic()
+    check(load().gbsv_set_c128_arith(C128_ARITH[mode]), "set_c128_arith")
+    return prev
+
+
+def complex128_arithmetic() -> str:
+    code = int(load().gbsv_get_c128_arith())
+    return {v: k for k, v in C128_ARITH.items()}[code]
 
 
 def qubit_array(qubits):

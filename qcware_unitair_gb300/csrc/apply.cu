@@ -17,8 +17,10 @@
 #include <stdio.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 
 namespace gbsv {
 
@@ -32,6 +34,7 @@ struct DenseArgs {
   int ins_pos[2];        // their bit positions, ascending
   int64_t hstride[2];    // amplitude offset selected by chunk bit 0 / 1
   int log_v;             // log2(V)
+  int df;                // complex128: double-float pairs (1) or FP64 (0)
 };
 
 template <typename C, int NR, int K, int RB0, int RB1>
@@ -68,39 +71,77 @@ __device__ __forceinline__ void apply_regs(C* r, const C* m) {
   }
 }
 
-// complex128: GB300 issues FP64 at a small fraction of its FP32 rate, so a
-// gate's FP64 work, not HBM, bounded the complex128 path.  The matrix's
-// kind (permutation, diagonal, anti-diagonal, real, real diagonal with
-// imaginary off-diagonal, controlled 2x2, general) is found once per thread
-// and each kind runs its own loop with only the FP64 operations it needs.
-// The kind is the same for a whole warp when the operator is shared, and
-// the loops are too large to be turned into selects, so no FP64 work is
-// issued for the other kinds.  Roundings are those of cmul / cmad.
-constexpr int EC_ZERO = 0, EC_ONE = 1, EC_REAL = 2, EC_IMAG = 3,
-              EC_FULL = 4;
+// complex128: GB300 issues FP64 at about 1/64 of its FP32 rate, so a gate
+// whose 2x2 update runs in FP64 is bound by the FP64 pipe, not by HBM.
+// The kernel therefore (1) finds the shared operator's structure once per
+// block (warp 0 classifies the entries from their bit patterns and splits
+// them into exact float triples in shared memory), (2) runs each kind's own
+// loop, so permutations and the entries 0, +-1, +-i cost no arithmetic at
+// all, and (3) does the remaining arithmetic in double-float pairs on the
+// FP32 pipe (dfloat.cuh), with native FP64 kept for threads whose
+// amplitudes lie outside the pair range, for per-state operators, and for
+// the whole engine when gbsv_set_c128_arith selects it.
+constexpr int EC_ZERO = 0, EC_ONE = 1, EC_MONE = 2, EC_I = 3, EC_MI = 4,
+              EC_REAL = 5, EC_IMAG = 6, EC_FULL = 7;
+// classes up to EC_MI need no arithmetic
+__device__ __forceinline__ bool ec_real(int c) {
+  return c <= EC_MONE || c == EC_REAL;
+}
+__device__ __forceinline__ bool ec_imag(int c) {
+  return c == EC_I || c == EC_MI || c == EC_IMAG;
+}
 
 // From the bit patterns (integer compares: an FP64 compare costs an FP64
 // issue slot; +0 and -0 are both zero)
 template <typename C>
 __device__ __forceinline__ int entry_class(const C& m) {
+  constexpr unsigned long long P1 = 0x3FF0000000000000ull;  // +1.0
+  constexpr unsigned long long M1 = 0xBFF0000000000000ull;  // -1.0
   const unsigned long long xb = __double_as_longlong(m.x);
   const unsigned long long yb = __double_as_longlong(m.y);
   const bool xz = (xb << 1) == 0, yz = (yb << 1) == 0;
-  if (yz) return xz ? EC_ZERO : (xb == 0x3FF0000000000000ull ? EC_ONE : EC_REAL);
-  return xz ? EC_IMAG : EC_FULL;
+  if (yz)
+    return xz ? EC_ZERO : xb == P1 ? EC_ONE : xb == M1 ? EC_MONE : EC_REAL;
+  if (xz) return yb == P1 ? EC_I : yb == M1 ? EC_MI : EC_IMAG;
+  return EC_FULL;
 }
 
-// r[i] *= m for the registers i with (i & MASK) == PAT
+// -x by flipping the sign bit (an integer operation)
+__device__ __forceinline__ double dneg(double x) {
+  return __hiloint2double(__double2hiint(x) ^ (int)0x80000000,
+                          __double2loint(x));
+}
+
+// r *= m for the classes that need no arithmetic (cls <= EC_MI); the
+// results equal the FP64 products.
+template <typename C>
+__device__ __forceinline__ void scale_exact(C& r, int cls) {
+  const double x = r.x, y = r.y;
+  switch (cls) {
+    case EC_ZERO:
+      r.x = r.y = 0;
+      return;
+    case EC_MONE:
+      r.x = dneg(x);
+      r.y = dneg(y);
+      return;
+    case EC_I:  // i (x + iy) = -y + ix
+      r.x = dneg(y);
+      r.y = x;
+      return;
+    case EC_MI:
+      r.x = y;
+      r.y = dneg(x);
+      return;
+    default:
+      return;
+  }
+}
+
+// r[i] *= m for the registers i with (i & MASK) == PAT; FP64 form
 template <typename C, int NR, int MASK, int PAT>
 __device__ __forceinline__ void scale_sel(C* r, const C& m, int cls) {
   switch (cls) {
-    case EC_ONE:
-      return;
-    case EC_ZERO:
-#pragma unroll
-      for (int i = 0; i < NR; ++i)
-        if ((i & MASK) == PAT) r[i].x = r[i].y = 0;
-      return;
     case EC_REAL:
 #pragma unroll
       for (int i = 0; i < NR; ++i)
@@ -118,10 +159,56 @@ __device__ __forceinline__ void scale_sel(C* r, const C& m, int cls) {
           r[i].y = m.y * t.x;
         }
       return;
-    default:
+    case EC_FULL:
 #pragma unroll
       for (int i = 0; i < NR; ++i)
         if ((i & MASK) == PAT) r[i] = cmul(m, r[i]);
+      return;
+    default:
+      if (cls == EC_ONE) return;
+#pragma unroll
+      for (int i = 0; i < NR; ++i)
+        if ((i & MASK) == PAT) scale_exact(r[i], cls);
+      return;
+  }
+}
+
+// the same in double-float pairs (e: the entry's exact triple)
+template <typename C, int NR, int MASK, int PAT>
+__device__ __forceinline__ void scale_sel_df(C* r, const DEC& e, int cls) {
+  switch (cls) {
+    case EC_REAL:
+#pragma unroll
+      for (int i = 0; i < NR; ++i)
+        if ((i & MASK) == PAT) {
+          const DC y = df_rmul(e.re, df_split2(r[i].x, r[i].y));
+          r[i].x = df_join(y.re);
+          r[i].y = df_join(y.im);
+        }
+      return;
+    case EC_IMAG:
+#pragma unroll
+      for (int i = 0; i < NR; ++i)
+        if ((i & MASK) == PAT) {
+          const DC y = df_imul(e.im, df_split2(r[i].x, r[i].y));
+          r[i].x = df_join(y.re);
+          r[i].y = df_join(y.im);
+        }
+      return;
+    case EC_FULL:
+#pragma unroll
+      for (int i = 0; i < NR; ++i)
+        if ((i & MASK) == PAT) {
+          const DC y = df_cmul(e, df_split2(r[i].x, r[i].y));
+          r[i].x = df_join(y.re);
+          r[i].y = df_join(y.im);
+        }
+      return;
+    default:
+      if (cls == EC_ONE) return;
+#pragma unroll
+      for (int i = 0; i < NR; ++i)
+        if ((i & MASK) == PAT) scale_exact(r[i], cls);
       return;
   }
 }
@@ -133,20 +220,33 @@ __device__ __forceinline__ int kind_2x2(int c0, int c1, int c2, int c3) {
   if (c1 == EC_ZERO && c2 == EC_ZERO) return K1_DIAG;
   if (c0 == EC_ZERO && c3 == EC_ZERO)
     return c1 == EC_ONE && c2 == EC_ONE ? K1_PERM : K1_ANTI;
-  const bool re = c0 <= EC_REAL && c1 <= EC_REAL && c2 <= EC_REAL &&
-                  c3 <= EC_REAL;
-  if (re) return K1_REAL;
-  if (c0 <= EC_REAL && c3 <= EC_REAL && c1 == EC_IMAG && c2 == EC_IMAG)
-    return K1_RX;
+  if (ec_real(c0) && ec_real(c1) && ec_real(c2) && ec_real(c3))
+    return K1_REAL;
+  if (ec_real(c0) && ec_real(c3) && ec_imag(c1) && ec_imag(c2)) return K1_RX;
   return K1_FULL;
 }
 
+// Does a 2x2 of this kind and these classes need arithmetic?
+__device__ __forceinline__ bool arith_2x2(int kind, const int* c) {
+  switch (kind) {
+    case K1_PERM:
+      return false;
+    case K1_DIAG:
+      return c[0] > EC_MI || c[3] > EC_MI;
+    case K1_ANTI:
+      return c[1] > EC_MI || c[2] > EC_MI;
+    default:
+      return true;
+  }
+}
+
 // The 2x2 (m0 m1; m2 m3) on register bit T, for the registers i with
-// (i & CM) == CV (a control pattern; 0, 0 for none).
+// (i & CM) == CV (a control pattern; 0, 0 for none); c: the entries'
+// classes.  FP64 form.
 template <typename C, int NR, int T, int CM, int CV>
 __device__ __forceinline__ void apply_2x2(C* r, const C& m0, const C& m1,
                                           const C& m2, const C& m3, int kind,
-                                          int c0, int c3) {
+                                          const int* c) {
   constexpr int B = 1 << T;
   switch (kind) {
     case K1_PERM:
@@ -159,17 +259,19 @@ __device__ __forceinline__ void apply_2x2(C* r, const C& m0, const C& m1,
       }
       return;
     case K1_DIAG:
-      scale_sel<C, NR, B | CM, CV>(r, m0, c0);
-      scale_sel<C, NR, B | CM, B | CV>(r, m3, c3);
+      scale_sel<C, NR, B | CM, CV>(r, m0, c[0]);
+      scale_sel<C, NR, B | CM, B | CV>(r, m3, c[3]);
       return;
-    case K1_ANTI:
+    case K1_ANTI:  // swap, then scale by m1 (row 0) and m2 (row 1)
 #pragma unroll
       for (int i = 0; i < NR; ++i) {
         if ((i & B) || (i & CM) != CV) continue;
-        const C a0 = r[i], a1 = r[i | B];
-        r[i] = cmul(m1, a1);
-        r[i | B] = cmul(m2, a0);
+        const C t = r[i];
+        r[i] = r[i | B];
+        r[i | B] = t;
       }
+      scale_sel<C, NR, B | CM, CV>(r, m1, c[1]);
+      scale_sel<C, NR, B | CM, B | CV>(r, m2, c[2]);
       return;
     case K1_REAL:
 #pragma unroll
@@ -205,41 +307,100 @@ __device__ __forceinline__ void apply_2x2(C* r, const C& m0, const C& m1,
   }
 }
 
-// Precomputed structure of a complex128 operator (see apply_c128).
+// The same in double-float pairs, entries from their exact triples.
+template <typename C, int NR, int T, int CM, int CV>
+__device__ __forceinline__ void apply_2x2_df(C* r, const DEC& e0,
+                                             const DEC& e1, const DEC& e2,
+                                             const DEC& e3, int kind,
+                                             const int* c) {
+  constexpr int B = 1 << T;
+  switch (kind) {
+    case K1_PERM:
+#pragma unroll
+      for (int i = 0; i < NR; ++i) {
+        if ((i & B) || (i & CM) != CV) continue;
+        const C t = r[i];
+        r[i] = r[i | B];
+        r[i | B] = t;
+      }
+      return;
+    case K1_DIAG:
+      scale_sel_df<C, NR, B | CM, CV>(r, e0, c[0]);
+      scale_sel_df<C, NR, B | CM, B | CV>(r, e3, c[3]);
+      return;
+    case K1_ANTI:
+#pragma unroll
+      for (int i = 0; i < NR; ++i) {
+        if ((i & B) || (i & CM) != CV) continue;
+        const C t = r[i];
+        r[i] = r[i | B];
+        r[i | B] = t;
+      }
+      scale_sel_df<C, NR, B | CM, CV>(r, e1, c[1]);
+      scale_sel_df<C, NR, B | CM, B | CV>(r, e2, c[2]);
+      return;
+    default:
+#pragma unroll
+      for (int i = 0; i < NR; ++i) {
+        if ((i & B) || (i & CM) != CV) continue;
+        const DC a0 = df_split2(r[i].x, r[i].y);
+        const DC a1 = df_split2(r[i | B].x, r[i | B].y);
+        DC y0, y1;
+        if (kind == K1_REAL) {
+          y0 = df_row2_real(e0.re, a0, e1.re, a1);
+          y1 = df_row2_real(e2.re, a0, e3.re, a1);
+        } else if (kind == K1_RX) {
+          y0 = df_row2_rx(e0.re, a0, e1.im, a1);
+          y1 = df_row2_rx(e3.re, a1, e2.im, a0);
+        } else {
+          y0 = df_row2(e0, a0, e1, a1);
+          y1 = df_row2(e2, a0, e3, a1);
+        }
+        r[i].x = df_join(y0.re);
+        r[i].y = df_join(y0.im);
+        r[i | B].x = df_join(y1.re);
+        r[i | B].y = df_join(y1.im);
+      }
+      return;
+  }
+}
+
+// Structure of a complex128 operator, found once per block.
 struct OpKind {
-  int kind;     // K1_* for 2x2; for 4x4: 0 general, 1 permutation,
-                // 2 diagonal, 3 controlled 2x2
+  int kind;     // K1_* for 2x2; for 4x4: 0 general, 1 monomial (one
+                // nonzero entry per row and column), 2 diagonal,
+                // 3 controlled 2x2
   int sub;      // 4x4 controlled: K1_* of the 2x2 block
-  int c[4];     // classes of the four diagonal (or block) entries
-  int perm;     // 4x4 permutation: source column of row j in bits 2j..2j+1
+  int c[4];     // classes of the 2x2's entries m0..m3 / of the 4x4's
+                // row entries (monomial) or diagonal / of the controlled
+                // block's entries
+  int perm;     // 4x4 monomial: column of row j's entry in bits 2j..2j+1
+  int arith;    // 1 if applying it needs arithmetic
 };
 
-template <typename C, int K>
-__device__ __forceinline__ OpKind classify_op(const C* m) {
+template <int K>
+__device__ __forceinline__ OpKind classify_classes(const int* cl) {
   OpKind k{};
   if constexpr (K == 1) {
-    const int c0 = entry_class(m[0]), c1 = entry_class(m[1]),
-              c2 = entry_class(m[2]), c3 = entry_class(m[3]);
-    k.kind = kind_2x2(c0, c1, c2, c3);
-    k.c[0] = c0;
-    k.c[3] = c3;
+    k.kind = kind_2x2(cl[0], cl[1], cl[2], cl[3]);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) k.c[j] = cl[j];
+    k.arith = arith_2x2(k.kind, k.c);
     return k;
   } else {
-    int cl[16];
-#pragma unroll
-    for (int j = 0; j < 16; ++j) cl[j] = entry_class(m[j]);
-    bool diag = true, perm = true, ctrl = true;
-    int pm = 0;
+    bool diag = true, mono = true, ctrl = true;
+    int pm = 0, cols = 0, rc[4];
 #pragma unroll
     for (int row = 0; row < 4; ++row) {
-      int ones = 0, nz = 0, col = 0;
+      int nz = 0, col = 0;
+      rc[row] = EC_ZERO;
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int c = cl[4 * row + j];
         if (c != EC_ZERO) {
           ++nz;
           col = j;
-          if (c == EC_ONE) ++ones;
+          rc[row] = c;
           if (j != row) diag = false;
           // controlled: identity on rows 0, 1; rows 2, 3 inside cols 2, 3
           if (row < 2 ? (j != row || c != EC_ONE) : j < 2) ctrl = false;
@@ -247,23 +408,37 @@ __device__ __forceinline__ OpKind classify_op(const C* m) {
           ctrl = false;
         }
       }
-      if (!(nz == 1 && ones == 1)) perm = false;
+      if (nz != 1) mono = false;
+      cols |= 1 << col;
       pm |= col << (2 * row);
     }
-    if (perm) {
+    if (cols != 15) mono = false;
+    if (mono && !diag) {
       k.kind = 1;
       k.perm = pm;
+      k.arith = 0;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        k.c[j] = rc[j];
+        if (rc[j] > EC_MI) k.arith = 1;
+      }
     } else if (diag) {
       k.kind = 2;
 #pragma unroll
       for (int j = 0; j < 4; ++j) k.c[j] = cl[5 * j];
+      k.arith = k.c[0] > EC_MI || k.c[1] > EC_MI || k.c[2] > EC_MI ||
+                k.c[3] > EC_MI;
     } else if (ctrl) {
       k.kind = 3;
-      k.sub = kind_2x2(cl[10], cl[11], cl[14], cl[15]);
       k.c[0] = cl[10];
+      k.c[1] = cl[11];
+      k.c[2] = cl[14];
       k.c[3] = cl[15];
+      k.sub = kind_2x2(k.c[0], k.c[1], k.c[2], k.c[3]);
+      k.arith = arith_2x2(k.sub, k.c);
     } else {
       k.kind = 0;
+      k.arith = 1;
     }
     return k;
   }
@@ -276,30 +451,45 @@ __device__ __forceinline__ C pick4(const C* v, int j) {
   return (j & 2) ? hi : lo;
 }
 
+template <typename C, int NR, int RB0, int RB1>
+__device__ __forceinline__ void permute4(C* r, int perm) {
+  constexpr int M0 = 1 << RB0, M1 = 1 << RB1;
+#pragma unroll
+  for (int i = 0; i < NR; ++i) {
+    if (i & (M0 | M1)) continue;
+    const int idx[4] = {i, i | M1, i | M0, i | M0 | M1};
+    C v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) v[j] = r[idx[j]];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) r[idx[j]] = pick4(v, (perm >> (2 * j)) & 3);
+  }
+}
+
 // Matrix index bit 1 (K = 2: the first target) is register bit RB0, bit 0
-// register bit RB1.
+// register bit RB1.  FP64 form.
 template <typename C, int NR, int K, int RB0, int RB1>
 __device__ __forceinline__ void apply_c128(C* r, const C* m,
                                            const OpKind& k) {
   if constexpr (K == 1) {
-    apply_2x2<C, NR, RB0, 0, 0>(r, m[0], m[1], m[2], m[3], k.kind, k.c[0],
-                                k.c[3]);
+    apply_2x2<C, NR, RB0, 0, 0>(r, m[0], m[1], m[2], m[3], k.kind, k.c);
   } else {
     constexpr int M0 = 1 << RB0, M1 = 1 << RB1;
     switch (k.kind) {
-      case 1:  // permutation: row j takes column perm_j
-#pragma unroll
-        for (int i = 0; i < NR; ++i) {
-          if (i & (M0 | M1)) continue;
-          const int idx[4] = {i, i | M1, i | M0, i | M0 | M1};
-          C v[4];
-#pragma unroll
-          for (int j = 0; j < 4; ++j) v[j] = r[idx[j]];
-#pragma unroll
-          for (int j = 0; j < 4; ++j)
-            r[idx[j]] = pick4(v, (k.perm >> (2 * j)) & 3);
+      case 1: {  // monomial: row j takes column perm_j, times its entry
+        permute4<C, NR, RB0, RB1>(r, k.perm);
+        if (k.c[0] != EC_ONE || k.c[1] != EC_ONE || k.c[2] != EC_ONE ||
+            k.c[3] != EC_ONE) {
+          scale_sel<C, NR, M0 | M1, 0>(r, pick4(m, k.perm & 3), k.c[0]);
+          scale_sel<C, NR, M0 | M1, M1>(r, pick4(m + 4, (k.perm >> 2) & 3),
+                                        k.c[1]);
+          scale_sel<C, NR, M0 | M1, M0>(r, pick4(m + 8, (k.perm >> 4) & 3),
+                                        k.c[2]);
+          scale_sel<C, NR, M0 | M1, M0 | M1>(
+              r, pick4(m + 12, (k.perm >> 6) & 3), k.c[3]);
         }
         return;
+      }
       case 2:  // diagonal
         scale_sel<C, NR, M0 | M1, 0>(r, m[0], k.c[0]);
         scale_sel<C, NR, M0 | M1, M1>(r, m[5], k.c[1]);
@@ -308,7 +498,7 @@ __device__ __forceinline__ void apply_c128(C* r, const C* m,
         return;
       case 3:  // controlled: the lower-right 2x2 where bit RB0 is set
         apply_2x2<C, NR, RB1, M0, M0>(r, m[10], m[11], m[14], m[15], k.sub,
-                                      k.c[0], k.c[3]);
+                                      k.c);
         return;
       default:
         apply_regs<C, NR, K, RB0, RB1>(r, m);
@@ -317,24 +507,132 @@ __device__ __forceinline__ void apply_c128(C* r, const C* m,
   }
 }
 
+// The same in double-float pairs (e: the entries' exact triples).
+template <typename C, int NR, int K, int RB0, int RB1>
+__device__ __forceinline__ void apply_c128_df(C* r, const DEC* e,
+                                              const OpKind& k) {
+  if constexpr (K == 1) {
+    apply_2x2_df<C, NR, RB0, 0, 0>(r, e[0], e[1], e[2], e[3], k.kind, k.c);
+  } else {
+    constexpr int M0 = 1 << RB0, M1 = 1 << RB1;
+    switch (k.kind) {
+      case 1:
+        permute4<C, NR, RB0, RB1>(r, k.perm);
+        if (k.c[0] != EC_ONE || k.c[1] != EC_ONE || k.c[2] != EC_ONE ||
+            k.c[3] != EC_ONE) {
+          scale_sel_df<C, NR, M0 | M1, 0>(r, e[k.perm & 3], k.c[0]);
+          scale_sel_df<C, NR, M0 | M1, M1>(r, e[4 + ((k.perm >> 2) & 3)],
+                                           k.c[1]);
+          scale_sel_df<C, NR, M0 | M1, M0>(r, e[8 + ((k.perm >> 4) & 3)],
+                                           k.c[2]);
+          scale_sel_df<C, NR, M0 | M1, M0 | M1>(
+              r, e[12 + ((k.perm >> 6) & 3)], k.c[3]);
+        }
+        return;
+      case 2:
+        scale_sel_df<C, NR, M0 | M1, 0>(r, e[0], k.c[0]);
+        scale_sel_df<C, NR, M0 | M1, M1>(r, e[5], k.c[1]);
+        scale_sel_df<C, NR, M0 | M1, M0>(r, e[10], k.c[2]);
+        scale_sel_df<C, NR, M0 | M1, M0 | M1>(r, e[15], k.c[3]);
+        return;
+      case 3:
+        apply_2x2_df<C, NR, RB1, M0, M0>(r, e[10], e[11], e[14], e[15],
+                                         k.sub, k.c);
+        return;
+      default:
+#pragma unroll
+        for (int i = 0; i < NR; ++i) {
+          if (i & (M0 | M1)) continue;
+          const int idx[4] = {i, i | M1, i | M0, i | M0 | M1};
+          DC a[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            a[j] = df_split2(r[idx[j]].x, r[idx[j]].y);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const DC y = df_row4(e + 4 * j, a);
+            r[idx[j]].x = df_join(y.re);
+            r[idx[j]].y = df_join(y.im);
+          }
+        }
+        return;
+    }
+  }
+}
+
+// The shared operator of a complex128 launch, one copy per warp in shared
+// memory.
+template <int D>
+struct C128Op {
+  OpKind k;
+  int pairs_ok;     // entries within the pair range
+  DEC e[D * D];     // exact triples, for the pairs
+  double2 raw[D * D];  // the entries, for the FP64 form
+};
+
+// Each warp fills its own copy (no block barrier): lane j loads entry j,
+// classifies and splits it; the classes reach every lane as three ballots
+// (one per class bit).
+template <typename C, int K>
+__device__ __forceinline__ void c128_prologue(const C* ops,
+                                              C128Op<1 << K>& op) {
+  constexpr int D = 1 << K;
+  const int lane = threadIdx.x & 31;
+  int cls = EC_ZERO;
+  uint32_t mag = 0;
+  if (lane < D * D) {
+    const C mj = __ldg(ops + lane);
+    cls = entry_class(mj);
+    op.e[lane] = df_entry2(mj.x, mj.y);
+    op.raw[lane] = mj;
+    mag = max(df_hiword(mj.x) & 0x7fffffffu, df_hiword(mj.y) & 0x7fffffffu);
+  }
+  const uint32_t mx = __reduce_max_sync(0xffffffffu, mag);
+  const uint32_t p0 = __ballot_sync(0xffffffffu, cls & 1);
+  const uint32_t p1 = __ballot_sync(0xffffffffu, cls & 2);
+  const uint32_t p2 = __ballot_sync(0xffffffffu, cls & 4);
+  int cl[D * D];
+#pragma unroll
+  for (int j = 0; j < D * D; ++j)
+    cl[j] = ((p0 >> j) & 1) | (((p1 >> j) & 1) << 1) | (((p2 >> j) & 1) << 2);
+  if (lane == 0) {
+    op.k = classify_classes<K>(cl);
+    op.pairs_ok = mx >= (DF_EMIN << 20) && mx < ((DF_EMAX + 1) << 20);
+  }
+  __syncwarp();
+}
+
+// Every amplitude component of the thread's registers within the pair
+// range (or zero).
+template <typename C, int NR>
+__device__ __forceinline__ bool pairs_in_range(const C* r) {
+  uint32_t mx = 0;  // largest exponent field (the split computes the same)
+#pragma unroll
+  for (int i = 0; i < NR; ++i)
+    mx = max(mx, max(df_hiword(r[i].x) & 0x7ff00000u,
+                     df_hiword(r[i].y) & 0x7ff00000u));
+  return mx < ((DF_EMAX + 1) << 20) && (mx == 0 || mx >= (DF_EMIN << 20));
+}
+
 // NH high targets (chunks per unit = 2^NH); RB0 / RB1 are the register-index
 // bits of the first / second target in matrix order.
 template <typename R, int V, int K, int NH, int RB0, int RB1>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, 3)
     dense_chunk_kernel(const Cx<R>* in, Cx<R>* out, const Cx<R>* ops,
                        DenseArgs a) {
   using C = Cx<R>;
   constexpr int NCH = 1 << NH;
   constexpr int NR = NCH * V;
   constexpr int D = 1 << K;
-  constexpr int TARGET = sizeof(R) == 4 ? 16 : 8;  // amplitudes per thread
+  // amplitudes per thread: complex128 keeps four so that the pair
+  // arithmetic fits about 72 registers (three blocks per SM)
+  constexpr int TARGET = sizeof(R) == 4 ? 16 : 4;
   constexpr int UNROLL = NR >= TARGET ? 1 : TARGET / NR;
+  constexpr bool kC128 = sizeof(R) == 8;
+  const bool shared_op = a.op_stride == 0;
 
   C m[D * D];
-  OpKind kind{};  // complex128: the operator's structure
-  constexpr bool kClassed = sizeof(R) == 8;
-  const bool shared_op = a.op_stride == 0;
-  if (shared_op) {
+  if (!kC128 && shared_op) {
 #pragma unroll
     for (int j = 0; j < D * D; ++j) m[j] = __ldg(ops + j);
   }
@@ -366,14 +664,23 @@ __global__ void __launch_bounds__(256, 2)
     }
   }
 
-  // complex128 with a shared operator: classified while the state loads
-  // are in flight, then one structured pass over every unit's registers
-  // (the target bits index within each unit's NR block; registers of units
-  // past the end are computed and not stored)
-  if constexpr (kClassed) {
+  // complex128 with a shared operator: warp 0 classifies it while the
+  // state loads are in flight, then one structured pass over every unit's
+  // registers (the target bits index within each unit's NR block;
+  // registers of units past the end are computed and not stored)
+  if constexpr (kC128) {
+    __shared__ C128Op<D> warp_op[256 / 32];
     if (shared_op) {
-      kind = classify_op<C, K>(m);
-      apply_c128<C, UNROLL * NR, K, RB0, RB1>(&reg[0][0], m, kind);
+      C128Op<D>& op = warp_op[threadIdx.x >> 5];
+      c128_prologue<C, K>(ops, op);
+      const OpKind kind = op.k;
+      bool pairs = a.df != 0;
+      if (pairs && kind.arith)
+        pairs = op.pairs_ok && pairs_in_range<C, UNROLL * NR>(&reg[0][0]);
+      if (pairs || !kind.arith)
+        apply_c128_df<C, UNROLL * NR, K, RB0, RB1>(&reg[0][0], op.e, kind);
+      else
+        apply_c128<C, UNROLL * NR, K, RB0, RB1>(&reg[0][0], op.raw, kind);
     }
   }
 #pragma unroll
@@ -385,7 +692,7 @@ __global__ void __launch_bounds__(256, 2)
 #pragma unroll
       for (int j = 0; j < D * D; ++j) m[j] = __ldg(mp + j);
       apply_regs<C, NR, K, RB0, RB1>(reg[u], m);
-    } else if constexpr (!kClassed) {
+    } else if constexpr (!kC128) {
       apply_regs<C, NR, K, RB0, RB1>(reg[u], m);
     }
     C* dst = out + obase[u];
@@ -395,6 +702,155 @@ __global__ void __launch_bounds__(256, 2)
       if (NH > 0 && (c & 1)) off += a.hstride[0];
       if (NH > 1 && (c & 2)) off += a.hstride[1];
       store_chunk<V>(dst + off, &reg[u][c * V]);
+    }
+  }
+}
+
+// complex128 with one operator shared by every state: a persistent kernel
+// in warp steps.  A warp step covers one block of 128 amplitudes: its
+// "inner" index bits are the gate's targets and the lowest other bits (7
+// in all), so the block is made of contiguous runs of at least 32
+// amplitudes (512 bytes).  Lanes copy the block lane-contiguously into the
+// warp's shared-memory slot with 16-byte cp.async copies, two steps ahead;
+// each lane then takes its two pairs (one qubit) or its quad (two qubits)
+// out of the slot, applies the gate in registers, puts the results back,
+// and the warp stores the block lane-contiguously.  The pair arithmetic
+// needs over 100 registers, which leaves no room to hold loads in flight in
+// registers; through shared memory each SM keeps 64 KB of loads in flight
+// (two blocks of eight warps, two steps of 2 KB ahead) while its warps
+// compute.  Lanes never share a pair, so each lane writes back only what
+// it read.  Warp steps cover disjoint amplitudes, so in-place updates are
+// safe.
+constexpr int C128_STAGES = 3;    // slots per warp: two in flight, one in use
+constexpr int C128_THREADS = 256;
+constexpr int C128_BLOCK = 128;   // amplitudes per warp step
+
+struct StreamArgs {
+  uint64_t total_steps;  // num_states << (n - 7)
+  int log_steps;         // n - 7
+  int df;                // double-float pairs (1) or FP64 (0)
+  int64_t in_stride;     // amplitudes between input states (0 = broadcast)
+  int n;
+  int inner[7];          // inner bit positions, ascending: 0 .. low - 1,
+  int low;               // then the targets above that run (hpos)
+  int nhigh;
+  int hpos[2];
+  int b0, b1;            // inner index of the first / second target
+};
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s),
+               "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait1() {
+  asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+}
+
+template <int K>
+__global__ void __launch_bounds__(C128_THREADS, 2)
+    dense_c128_stream_kernel(const double2* in, double2* out,
+                             const double2* ops, StreamArgs a) {
+  using C = double2;
+  constexpr int D = 1 << K;
+  extern __shared__ __align__(16) double2 slots[];  // [warp][stage][128]
+  __shared__ uint32_t loc_off[C128_BLOCK];  // inner index -> offset
+  __shared__ C128Op<D> warp_op[C128_THREADS / 32];
+
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  for (int j = t; j < C128_BLOCK; j += C128_THREADS) {
+    uint32_t off = 0;
+#pragma unroll
+    for (int q = 0; q < 7; ++q)
+      if ((j >> q) & 1) off |= 1u << a.inner[q];
+    loc_off[j] = off;
+  }
+  __syncthreads();
+
+  C* const slot = slots + warp * (C128_STAGES * C128_BLOCK);
+  const uint64_t nw = (uint64_t)gridDim.x * (C128_THREADS / 32);
+  const uint64_t smask = (uint64_t(1) << a.log_steps) - 1;
+
+  // amplitude offset of warp step ws's block (inner bits zero)
+  auto block_base = [&](uint64_t ws, uint64_t& st) {
+    st = ws >> a.log_steps;
+    uint64_t x = (ws & smask) << a.low;
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+      if (j < a.nhigh) x = insert_zero(x, a.hpos[j]);
+    return x;
+  };
+  auto issue = [&](uint64_t ws, int stage) {
+    if (ws < a.total_steps) {
+      uint64_t st;
+      const uint64_t x = block_base(ws, st);
+      const C* src = in + st * a.in_stride + x;
+#pragma unroll
+      for (int i = 0; i < C128_BLOCK / 32; ++i) {
+        const int j = lane + 32 * i;
+        cp_async16(&slot[stage * C128_BLOCK + j], src + loc_off[j]);
+      }
+    }
+    cp_async_commit();
+  };
+
+  // the lane's amplitudes inside the block, in matrix order
+  int idx[4];
+  if constexpr (K == 1) {
+    const int m = 1 << a.b0;
+    idx[0] = (int)insert_zero((uint64_t)lane, a.b0);
+    idx[1] = idx[0] | m;
+    idx[2] = (int)insert_zero((uint64_t)lane + 32, a.b0);
+    idx[3] = idx[2] | m;
+  } else {
+    const int lo = min(a.b0, a.b1), hi = max(a.b0, a.b1);
+    const int base = (int)insert_zero(insert_zero((uint64_t)lane, lo), hi);
+    idx[0] = base;
+    idx[1] = base | (1 << a.b1);
+    idx[2] = base | (1 << a.b0);
+    idx[3] = base | (1 << a.b0) | (1 << a.b1);
+  }
+  constexpr int RB0 = K == 1 ? 0 : 1, RB1 = 0;
+
+  uint64_t ws = (uint64_t)blockIdx.x * (C128_THREADS / 32) + warp;
+  issue(ws, 0);
+  issue(ws + nw, 1);
+  C128Op<D>& op = warp_op[warp];
+  c128_prologue<C, K>(ops, op);
+  const OpKind kind = op.k;
+  const bool pairs_mode = a.df != 0 && op.pairs_ok;
+
+  for (int k = 0; ws < a.total_steps; ++k, ws += nw) {
+    C* const S = slot + (k % C128_STAGES) * C128_BLOCK;
+    cp_async_wait1();
+    __syncwarp();  // every lane's copies of this step have landed, and
+                   // every lane is done with the slot reused below
+    issue(ws + 2 * nw, (k + 2) % C128_STAGES);
+    C r[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) r[j] = S[idx[j]];
+
+    bool pairs = pairs_mode;
+    if (pairs && kind.arith) pairs = pairs_in_range<C, 4>(r);
+    if (pairs || !kind.arith)
+      apply_c128_df<C, 4, K, RB0, RB1>(r, op.e, kind);
+    else
+      apply_c128<C, 4, K, RB0, RB1>(r, op.raw, kind);
+
+#pragma unroll
+    for (int j = 0; j < 4; ++j) S[idx[j]] = r[j];
+    __syncwarp();
+    uint64_t st;
+    const uint64_t x = block_base(ws, st);
+    C* dst = out + (st << a.n) + x;
+#pragma unroll
+    for (int i = 0; i < C128_BLOCK / 32; ++i) {
+      const int j = lane + 32 * i;
+      __stcs(dst + loc_off[j], S[j]);
     }
   }
 }
@@ -554,7 +1010,7 @@ template <typename R, int V, int K, int NH, int RB0, int RB1>
 static int launch_chunk(const void* in, void* out, const void* ops,
                         const DenseArgs& a, cudaStream_t st) {
   constexpr int NR = (1 << NH) * V;
-  constexpr int TARGET = sizeof(R) == 4 ? 16 : 8;
+  constexpr int TARGET = sizeof(R) == 4 ? 16 : 4;
   constexpr int UNROLL = NR >= TARGET ? 1 : TARGET / NR;
   const uint64_t per_block = (uint64_t)UNROLL * 256;
   const uint64_t blocks = (a.total_units + per_block - 1) / per_block;
@@ -565,6 +1021,67 @@ static int launch_chunk(const void* in, void* out, const void* ops,
       static_cast<const Cx<R>*>(in), static_cast<Cx<R>*>(out),
       static_cast<const Cx<R>*>(ops), a);
   return after_launch("dense_chunk_kernel");
+}
+
+// complex128, shared operator, n >= 7: the warp-step streaming kernel.
+static int launch_c128_stream(const void* in, void* out, int n,
+                              int64_t num_states, int64_t in_stride,
+                              const void* ops, const int* pos, int k,
+                              cudaStream_t st) {
+  StreamArgs a{};
+  a.n = n;
+  a.log_steps = n - 7;
+  a.total_steps = (uint64_t)num_states << a.log_steps;
+  a.in_stride = in_stride;
+  a.df = c128_arith() == GBSV_C128_PAIRS;
+  // inner bits: the targets and the lowest other bits, 7 in all
+  uint64_t inner_mask = 0;
+  for (int j = 0; j < k; ++j) inner_mask |= uint64_t(1) << pos[j];
+  for (int b = 0; __builtin_popcountll(inner_mask) < 7; ++b)
+    inner_mask |= uint64_t(1) << b;
+  int q = 0;
+  for (int b = 0; b < n; ++b)
+    if ((inner_mask >> b) & 1) {
+      if (b == pos[0]) a.b0 = q;
+      if (k == 2 && b == pos[1]) a.b1 = q;
+      a.inner[q++] = b;
+    }
+  while (a.low < 7 && a.inner[a.low] == a.low) ++a.low;
+  a.nhigh = 7 - a.low;  // at most the two targets
+  for (int j = 0; j < a.nhigh; ++j) a.hpos[j] = a.inner[a.low + j];
+  constexpr size_t smem = (size_t)(C128_THREADS / 32) * C128_STAGES *
+                          C128_BLOCK * sizeof(double2);
+  const void* fn = k == 1 ? (const void*)dense_c128_stream_kernel<1>
+                          : (const void*)dense_c128_stream_kernel<2>;
+  // the shared-memory opt-in, once per device and kernel (a race only
+  // repeats it)
+  static std::atomic<uint64_t> attr_set[2];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const uint64_t bit = uint64_t(1) << (dev & 63);
+  if (!(attr_set[k - 1].load(std::memory_order_relaxed) & bit)) {
+    const cudaError_t e = cudaFuncSetAttribute(
+        fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+      return set_error(GBSV_ERR_CUDA, "dense_c128_stream_kernel: %s",
+                       cudaGetErrorString(e));
+    attr_set[k - 1].fetch_or(bit, std::memory_order_relaxed);
+  }
+  const uint64_t warps = C128_THREADS / 32;
+  uint64_t blocks = (a.total_steps + warps - 1) / warps;
+  const uint64_t cap = (uint64_t)sm_count() * 2;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  const double2* i2 = static_cast<const double2*>(in);
+  double2* o2 = static_cast<double2*>(out);
+  const double2* m2 = static_cast<const double2*>(ops);
+  if (k == 1)
+    dense_c128_stream_kernel<1>
+        <<<(unsigned)blocks, C128_THREADS, smem, st>>>(i2, o2, m2, a);
+  else
+    dense_c128_stream_kernel<2>
+        <<<(unsigned)blocks, C128_THREADS, smem, st>>>(i2, o2, m2, a);
+  return after_launch("dense_c128_stream_kernel");
 }
 
 // Select the template instance for (V, K, NH, RB0, RB1).
@@ -608,6 +1125,10 @@ static int apply_small(const void* in, void* out, int dtype, int n,
                        int64_t op_stride, const int* pos, int k,
                        cudaStream_t st) {
   const int amp = dtype_bytes(dtype);
+  if (dtype == GBSV_C128 && op_stride == 0 && n >= 7 &&
+      (uintptr_t)in % 16 == 0 && (uintptr_t)out % 16 == 0)
+    return launch_c128_stream(in, out, n, num_states, in_stride, ops, pos, k,
+                              st);
   const int vfull = dtype == GBSV_C64 ? 4 : 2;
   const int log_vfull = dtype == GBSV_C64 ? 2 : 1;
   int nh_full = 0;
@@ -641,6 +1162,7 @@ static int apply_small(const void* in, void* out, int dtype, int n,
   for (int j = 0; j < nh; ++j) a.ins_pos[j] = hpos[j];
   a.log_units = n - log_v - nh;
   a.total_units = (uint64_t)num_states << a.log_units;
+  a.df = c128_arith() == GBSV_C128_PAIRS;
   if (dtype == GBSV_C64)
     return dispatch_chunk<float>(V, k, nh, rb[0], rb[1], in, out, ops, a, st);
   return dispatch_chunk<double>(V, k, nh, rb[0], rb[1], in, out, ops, a, st);

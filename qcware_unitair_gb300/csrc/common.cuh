@@ -154,6 +154,8 @@ __device__ __forceinline__ void cp_async_wait_all() {
 // Records a launch and converts a pending CUDA error into a status.
 int after_launch(const char* what);
 int set_error(int status, const char* fmt, ...);
+// GBSV_C128_PAIRS or GBSV_C128_FP64 (gbsv_set_c128_arith)
+int c128_arith();
 inline int dtype_bytes(int dtype) {
   switch (dtype) {
     case GBSV_C64: return 8;

@@ -10,6 +10,9 @@
 namespace gbsv {
 
 static std::atomic<uint64_t> g_launches{0};
+static std::atomic<int> g_c128_arith{GBSV_C128_PAIRS};
+
+int c128_arith() { return g_c128_arith.load(std::memory_order_relaxed); }
 static thread_local char g_last_error[512] = "";
 
 int set_error(int status, const char* fmt, ...) {
@@ -43,6 +46,16 @@ extern "C" const char* gbsv_status_string(int status) {
     default: return "unknown status";
   }
 }
+
+extern "C" int gbsv_set_c128_arith(int mode) {
+  if (mode != GBSV_C128_PAIRS && mode != GBSV_C128_FP64)
+    return gbsv::set_error(GBSV_ERR_INVALID_ARG,
+                           "unknown complex128 arithmetic mode %d", mode);
+  gbsv::g_c128_arith.store(mode, std::memory_order_relaxed);
+  return GBSV_OK;
+}
+
+extern "C" int gbsv_get_c128_arith(void) { return gbsv::c128_arith(); }
 
 extern "C" const char* gbsv_last_error(void) { return gbsv::g_last_error; }
 
