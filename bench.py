@@ -731,17 +731,22 @@ def _wl_timed(fn):
     return e0.elapsed_time(e1)
 
 
-def wl_stage(n: int = 26, gates: int = 200, tensor_cores=None) -> float:
+def wl_stage(n: int = 26, gates: int = 200, tensor_cores=None,
+             dtype: str = "c64") -> float:
+    """A random circuit through fused stages (complex64, or complex128 in
+    the process's arithmetic mode)."""
     import torch
     from qcware_unitair_gb300.circuits import random_circuit, zero_state
     from qcware_unitair_gb300.fusion import Circuit
     dev = torch.device("cuda")
+    dt = torch.complex64 if dtype == "c64" else torch.complex128
     prog = Circuit.from_gates(n, random_circuit(n, gates, seed=0)).compile(
-        torch.complex64, dev, tensor_cores=tensor_cores)
-    psi = zero_state(n, (), torch.complex64, dev)
+        dt, dev, tensor_cores=tensor_cores)
+    psi = zero_state(n, (), dt, dev)
     ms = _wl_timed(lambda: prog.run(psi, inplace=True))
-    print(f"stage n={n} gates={gates} tensor_cores={prog.tensor_cores} "
-          f"passes={prog.num_passes} {ms:.3f} ms")
+    print(f"stage n={n} gates={gates} dtype={dtype} "
+          f"tensor_cores={prog.tensor_cores} passes={prog.num_passes} "
+          f"{ms:.3f} ms")
     return ms
 
 
@@ -897,6 +902,11 @@ def run_workload(argv):
         wl_stage(*(int(a) for a in args))
     elif what == "stage_reg":
         wl_stage(*(int(a) for a in args), tensor_cores=False)
+    elif what == "stage128":  # n gates [fp64]
+        import qcware_unitair_gb300 as ug
+        if len(args) > 2:
+            ug.set_complex128_arithmetic(args[2])
+        wl_stage(*(int(a) for a in args[:2]), dtype="c128")
     elif what == "gates":
         wl_gates(int(args[0]) if args else 24,
                  args[1] if len(args) > 1 else "H",

@@ -18,6 +18,7 @@
 // (unit u = l >> 1 is stored at u ^ ((u >> 3) & 7)) so pair updates on any
 // tile bit stay within the 2-wavefront minimum per warp.
 #include "common.cuh"
+#include "dfloat.cuh"
 
 #include <algorithm>
 
@@ -399,6 +400,7 @@ struct Stage2Args {
   int num_layouts;
   int nbuf;                // tile buffers in shared memory (1 or 2)
   int64_t num_states;
+  int df;                  // complex128 in double-float pairs
 };
 
 constexpr int TS_MAXG = 96;   // decoded gates resident per CTA
@@ -621,65 +623,143 @@ __device__ bool ts_relabel(TOp& o, int* perm, int& flip, int8_t& vm) {
 }
 
 // ----------------------------------------------------- register kernels --
-template <typename C, int NR, int K>
-__device__ __forceinline__ void ts_dense1(C* v, const C* mm) {
-  const C m0 = mm[0], m1 = mm[1], m2 = mm[2], m3 = mm[3];
+// The operations are written once over a value type V (the registers) and
+// an entry type E (the matrix values): V = E = float2 / double2 for
+// complex64 and FP64 complex128, V = DC (double-float pairs) and E = DEC
+// (exact float triples) for complex128 in pairs.  These overloads are the
+// arithmetic they share.
+template <typename C>
+__device__ __forceinline__ C op_row2(const C& m0, const C& x0, const C& m1,
+                                     const C& x1) {
+  return cmad(m1, x1, cmul(m0, x0));
+}
+template <typename C>
+__device__ __forceinline__ C op_row2_real(const C& m0, const C& x0,
+                                          const C& m1, const C& x1) {
+  C y;
+  y.x = fma(m0.x, x0.x, m1.x * x1.x);
+  y.y = fma(m0.x, x0.y, m1.x * x1.y);
+  return y;
+}
+template <typename C>
+__device__ __forceinline__ C op_mul(const C& m, const C& x) {
+  return cmul(m, x);
+}
+template <typename C>
+__device__ __forceinline__ C op_row4(const C* m, const C* x) {
+  C acc = czero<C>();
+  for (int k = 0; k < 4; ++k) acc = cmad(m[k], x[k], acc);
+  return acc;
+}
+template <typename C>
+__device__ __forceinline__ bool is_one(const C& f) {
+  return f.x == 1 && f.y == 0;
+}
+// thread scalar *= entry
+template <typename C>
+__device__ __forceinline__ C op_scal(const C& ts, const C& m) {
+  return cmul(ts, m);
+}
+// value *= thread scalar
+template <typename C>
+__device__ __forceinline__ C op_by_scal(const C& ts, const C& x) {
+  return cmul(ts, x);
+}
+
+__device__ __forceinline__ DC op_row2(const DEC& m0, const DC& x0,
+                                      const DEC& m1, const DC& x1) {
+  return df_row2<false>(m0, x0, m1, x1);
+}
+__device__ __forceinline__ DC op_row2_real(const DEC& m0, const DC& x0,
+                                           const DEC& m1, const DC& x1) {
+  return df_row2_real<false>(m0.re, x0, m1.re, x1);
+}
+__device__ __forceinline__ DC op_mul(const DEC& m, const DC& x) {
+  return df_cmul<false>(m, x);
+}
+__device__ __forceinline__ DC op_row4(const DEC* m, const DC* x) {
+  return df_row4<false>(m, x);
+}
+// 1 + 0i up to the last 5 bits of the real part (|x - 1| < 2^-48) and an
+// imaginary part below 2^-149: skipping such a factor costs less than the
+// pairs' own rounding
+__device__ __forceinline__ bool is_one(const DEC& f) {
+  return f.re.hi == 1.f && f.re.mid == 0.f && f.im.hi == 0.f;
+}
+__device__ __forceinline__ DC op_scal(const DC& ts, const DEC& m) {
+  return df_cmul<false>(m, ts);
+}
+// a pair as an exact triple (its low word in the middle)
+__device__ __forceinline__ DEC df_as_entry(const DC& x) {
+  DEC e;
+  e.re = DE{x.re.hi, x.re.lo, 0.f};
+  e.im = DE{x.im.hi, x.im.lo, 0.f};
+  return e;
+}
+__device__ __forceinline__ DC op_by_scal(const DC& ts, const DC& x) {
+  return df_cmul<false>(df_as_entry(ts), x);
+}
+__device__ __forceinline__ bool is_one(const DC& f) {
+  return f.re.hi == 1.f && f.re.lo == 0.f && f.im.hi == 0.f &&
+         f.im.lo == 0.f;
+}
+
+template <typename V, typename E, int NR, int K>
+__device__ __forceinline__ void ts_dense1(V* v, const E* mm) {
+  const E m0 = mm[0], m1 = mm[1], m2 = mm[2], m3 = mm[3];
 #pragma unroll
   for (int i = 0; i < NR; ++i) {
     if ((i >> K) & 1) continue;
-    const C x0 = v[i], x1 = v[i | (1 << K)];
-    v[i] = cmad(m1, x1, cmul(m0, x0));
-    v[i | (1 << K)] = cmad(m3, x1, cmul(m2, x0));
+    const V x0 = v[i], x1 = v[i | (1 << K)];
+    v[i] = op_row2(m0, x0, m1, x1);
+    v[i | (1 << K)] = op_row2(m2, x0, m3, x1);
   }
 }
 
-template <typename C, int NR, int K>
-__device__ __forceinline__ void ts_real1(C* v, const C* mm) {
-  const auto a00 = mm[0].x, a01 = mm[1].x, a10 = mm[2].x, a11 = mm[3].x;
+template <typename V, typename E, int NR, int K>
+__device__ __forceinline__ void ts_real1(V* v, const E* mm) {
+  const E m0 = mm[0], m1 = mm[1], m2 = mm[2], m3 = mm[3];
 #pragma unroll
   for (int i = 0; i < NR; ++i) {
     if ((i >> K) & 1) continue;
-    const C x0 = v[i], x1 = v[i | (1 << K)];
-    C y0, y1;
-    y0.x = fma(a00, x0.x, a01 * x1.x);
-    y0.y = fma(a00, x0.y, a01 * x1.y);
-    y1.x = fma(a10, x0.x, a11 * x1.x);
-    y1.y = fma(a10, x0.y, a11 * x1.y);
+    const V x0 = v[i], x1 = v[i | (1 << K)];
+    const V y0 = op_row2_real(m0, x0, m1, x1);
+    const V y1 = op_row2_real(m2, x0, m3, x1);
     v[i] = y0;
     v[i | (1 << K)] = y1;
   }
 }
 
-template <typename C, int NR, int K>
-__device__ __forceinline__ void ts_swap1(C* v) {
+template <typename V, int NR, int K>
+__device__ __forceinline__ void ts_swap1(V* v) {
 #pragma unroll
   for (int i = 0; i < NR; ++i) {
     if ((i >> K) & 1) continue;
-    const C t = v[i];
+    const V t = v[i];
     v[i] = v[i | (1 << K)];
     v[i | (1 << K)] = t;
   }
 }
 
-template <typename C, int NR, int K>
-__device__ __forceinline__ void ts_anti1(C* v, const C* mm) {
-  const C a = mm[1], b = mm[2];
+template <typename V, typename E, int NR, int K>
+__device__ __forceinline__ void ts_anti1(V* v, const E* mm) {
+  const E a = mm[1], b = mm[2];
 #pragma unroll
   for (int i = 0; i < NR; ++i) {
     if ((i >> K) & 1) continue;
-    const C x0 = v[i], x1 = v[i | (1 << K)];
-    v[i] = cmul(a, x1);
-    v[i | (1 << K)] = cmul(b, x0);
+    const V x0 = v[i], x1 = v[i | (1 << K)];
+    v[i] = op_mul(a, x1);
+    v[i | (1 << K)] = op_mul(b, x0);
   }
 }
 
 // X on register bit KT where register bit KC is 1
-template <typename C, int NR, int KC, int KT>
-__device__ __forceinline__ void ts_cx2(C* v) {
+template <typename V, int NR, int KC, int KT>
+__device__ __forceinline__ void ts_cx2(V* v) {
 #pragma unroll
   for (int i = 0; i < NR; ++i) {
     if (!((i >> KC) & 1) || (i >> KT) & 1) continue;
-    const C t = v[i];
+    const V t = v[i];
     v[i] = v[i | (1 << KT)];
     v[i | (1 << KT)] = t;
   }
@@ -691,30 +771,28 @@ __device__ __forceinline__ C sel4(const C* pm, int i) {
   const C hi = (i & 1) ? pm[3] : pm[2];
   return (i & 2) ? hi : lo;
 }
-
-template <typename C>
-__device__ __forceinline__ bool is_one(const C& f) {
-  return f.x == 1 && f.y == 0;
-}
+// triples stay in shared memory: an indexed load, not 18 selects
+__device__ __forceinline__ DEC sel4(const DEC* pm, int i) { return pm[i]; }
 
 // 4x4 (dense, or a permutation given by code) on register bits k0 (matrix
 // MSB) and k1 known only at run time: the registers go through a local
 // copy that is indexed at run time, so the register array itself is only
 // ever indexed by constants.
-template <typename C, int NR>
-__device__ __noinline__ void ts_generic2_mem(C* t, int k0, int k1, bool dense,
-                                             int code, const C* mm) {
+template <typename V, typename E, int NR>
+__device__ __noinline__ void ts_generic2_mem(V* t, int k0, int k1,
+                                             bool dense, int code,
+                                             const E* mm) {
   const int b0 = 1 << k0, b1 = 1 << k1;
   for (int i = 0; i < NR; ++i) {
     if (i & (b0 | b1)) continue;
     const int idx[4] = {i, i | b1, i | b0, i | b0 | b1};
-    C x[4];
+    V x[4];
     for (int k = 0; k < 4; ++k) x[k] = t[idx[k]];
     for (int r = 0; r < 4; ++r) {
       if (dense) {
-        C acc = czero<C>();
-        for (int k = 0; k < 4; ++k) acc = cmad(mm[4 * r + k], x[k], acc);
-        t[idx[r]] = acc;
+        E row[4];
+        for (int k = 0; k < 4; ++k) row[k] = mm[4 * r + k];
+        t[idx[r]] = op_row4(row, x);
       } else {
         t[idx[r]] = x[(code >> (2 * r)) & 3];
       }
@@ -722,39 +800,39 @@ __device__ __noinline__ void ts_generic2_mem(C* t, int k0, int k1, bool dense,
   }
 }
 
-template <typename C, int NR>
-__device__ __forceinline__ void ts_generic2(C* v, int k0, int k1, bool dense,
-                                            int code, const C* mm) {
-  C t[NR];
+template <typename V, typename E, int NR>
+__device__ __forceinline__ void ts_generic2(V* v, int k0, int k1, bool dense,
+                                            int code, const E* mm) {
+  V t[NR];
 #pragma unroll
   for (int i = 0; i < NR; ++i) t[i] = v[i];
-  ts_generic2_mem<C, NR>(t, k0, k1, dense, code, mm);
+  ts_generic2_mem<V, E, NR>(t, k0, k1, dense, code, mm);
 #pragma unroll
   for (int i = 0; i < NR; ++i) v[i] = t[i];
 }
 
 // diagonal on register bits k0 (index MSB), k1 known at run time
-template <typename C, int NR>
-__device__ __forceinline__ void ts_diag2_any(C* v, int k0, int k1,
-                                             const C* d) {
+template <typename V, typename E, int NR>
+__device__ __forceinline__ void ts_diag2_any(V* v, int k0, int k1,
+                                             const E* d) {
 #pragma unroll
   for (int i = 0; i < NR; ++i) {
     const int idx = (((i >> k0) & 1) << 1) | ((i >> k1) & 1);
-    const C f = sel4(d, idx);
-    if (!is_one(f)) v[i] = cmul(f, v[i]);
+    const E f = sel4(d, idx);
+    if (!is_one(f)) v[i] = op_mul(f, v[i]);
   }
 }
 
 // diag(f0, f1) on register bit K
-template <typename C, int NR, int K>
-__device__ __forceinline__ void ts_diag1(C* v, const C& f0, const C& f1) {
+template <typename V, typename E, int NR, int K>
+__device__ __forceinline__ void ts_diag1(V* v, const E& f0, const E& f1) {
   const bool one0 = is_one(f0), one1 = is_one(f1);
 #pragma unroll
   for (int i = 0; i < NR; ++i) {
     if ((i >> K) & 1) {
-      if (!one1) v[i] = cmul(f1, v[i]);
+      if (!one1) v[i] = op_mul(f1, v[i]);
     } else if (!one0) {
-      v[i] = cmul(f0, v[i]);
+      v[i] = op_mul(f0, v[i]);
     }
   }
 }
@@ -813,15 +891,13 @@ __device__ __forceinline__ void ts_load_vals(C* pm, const C* src) {
 }
 
 // Apply one decoded operation to a thread's registers.
-template <typename R, int RB>
-__device__ __forceinline__ void ts_apply(Cx<R>* v, const TOp& o,
-                                         const Cx<R>* pm,
-                                         const Cx<R>* mats, int tb,
-                                         uint64_t base, Cx<R>& ts) {
-  using C = Cx<R>;
+template <typename V, typename E, int RB>
+__device__ __forceinline__ void ts_apply(V* v, const TOp& o, const E* pm,
+                                         const E* mats, int tb,
+                                         uint64_t base, V& ts) {
   constexpr int NR = 1 << RB;
   const int op = o.op;
-  const C* mm = pm;
+  const E* mm = pm;
   if (op < TOP_DIAG1) {
     if ((tb & o.x) != o.x || (base & o.a) != o.b) return;
   }
@@ -836,16 +912,16 @@ __device__ __forceinline__ void ts_apply(Cx<R>* v, const TOp& o,
     const int fam = op / 5, kk = op - 5 * fam;
     switch (fam) {
       case TOP_DENSE1 / 5:
-        switch (kk) { TS_KS(0, (ts_dense1<C, NR, K>(v, mm))) }
+        switch (kk) { TS_KS(0, (ts_dense1<V, E, NR, K>(v, mm))) }
         break;
       case TOP_REAL1 / 5:
-        switch (kk) { TS_KS(0, (ts_real1<C, NR, K>(v, mm))) }
+        switch (kk) { TS_KS(0, (ts_real1<V, E, NR, K>(v, mm))) }
         break;
       case TOP_SWAP1 / 5:
-        switch (kk) { TS_KS(0, (ts_swap1<C, NR, K>(v))) }
+        switch (kk) { TS_KS(0, (ts_swap1<V, NR, K>(v))) }
         break;
       default:
-        switch (kk) { TS_KS(0, (ts_anti1<C, NR, K>(v, mm))) }
+        switch (kk) { TS_KS(0, (ts_anti1<V, E, NR, K>(v, mm))) }
         break;
     }
   } else if (op < TOP_DIAG1) {
@@ -857,19 +933,19 @@ __device__ __forceinline__ void ts_apply(Cx<R>* v, const TOp& o,
                                      : op - TOP_SWAP2;
       const int k0 = p >> 2, j = p & 3, k1 = j < k0 ? j : j + 1;
       const int code = op < TOP_SWAP2 ? o.code : 0xd8;
-      ts_generic2<C, NR>(v, k0, k1, op < TOP_PERM2, code, mats + o.moff);
+      ts_generic2<V, E, NR>(v, k0, k1, op < TOP_PERM2, code, mats + o.moff);
     } else {
-      switch (op - TOP_CX2) { TS_PS(0, (ts_cx2<C, NR, K0, K1>(v))) }
+      switch (op - TOP_CX2) { TS_PS(0, (ts_cx2<V, NR, K0, K1>(v))) }
     }
   } else if (op < TOP_DIAG2) {
-    const C f0 = sel4(pm, fixed), f1 = sel4(pm, fixed | o.code);
-    switch (op - TOP_DIAG1) { TS_KS(0, (ts_diag1<C, NR, K>(v, f0, f1))) }
+    const E f0 = sel4(pm, fixed), f1 = sel4(pm, fixed | o.code);
+    switch (op - TOP_DIAG1) { TS_KS(0, (ts_diag1<V, E, NR, K>(v, f0, f1))) }
   } else if (op < TOP_SCALAR) {
     const int p = op - TOP_DIAG2;
     const int k0 = p >> 2, j = p & 3, k1 = j < k0 ? j : j + 1;
-    ts_diag2_any<C, NR>(v, k0, k1, pm);
+    ts_diag2_any<V, E, NR>(v, k0, k1, pm);
   } else if (op == TOP_SCALAR) {
-    ts = cmul(ts, sel4(pm, fixed));
+    ts = op_scal(ts, sel4(pm, fixed));
   }
 }
 
@@ -880,16 +956,19 @@ __device__ __forceinline__ void ts_apply(Cx<R>* v, const TOp& o,
 #undef TS_PS
 
 // Operations [first, end) in order.
-template <typename R, int RB>
-__device__ __forceinline__ void ts_run(Cx<R>* v, const TOp* ops,
-                                       const Cx<R>* mats, int first, int end,
-                                       int tb, uint64_t base, Cx<R>& ts) {
-  using C = Cx<R>;
+template <typename V, typename E, int RB>
+__device__ __forceinline__ void ts_run(V* v, const TOp* ops, const E* mats,
+                                       int first, int end, int tb,
+                                       uint64_t base, V& ts) {
   for (int gi = first; gi < end; ++gi) {
     const TOp o = ts_load_op(&ops[gi]);
-    C pm[4];
-    ts_load_vals(pm, mats + o.moff);
-    ts_apply<R, RB>(v, o, pm, mats, tb, base, ts);
+    if constexpr (sizeof(E) == sizeof(DEC)) {  // triples: read in place
+      ts_apply<V, E, RB>(v, o, mats + o.moff, mats, tb, base, ts);
+    } else {
+      E pm[4];
+      ts_load_vals(pm, mats + o.moff);
+      ts_apply<V, E, RB>(v, o, pm, mats, tb, base, ts);
+    }
   }
 }
 
@@ -968,6 +1047,10 @@ __device__ __forceinline__ void fused_reg_body(const Cx<R>* in, Cx<R>* out,
   C* const S0 = reinterpret_cast<C*>(smem_raw);
   __shared__ TOp ops[TS_MAXG];
   __shared__ __align__(16) C mats[TS_MAXM + 4];
+  // complex128 in pairs: the values as exact float triples
+  constexpr bool kPairs = sizeof(R) == 8;
+  __shared__ DEC matsd[kPairs ? TS_MAXM + 4 : 1];
+  __shared__ int sh_pairs;
   __shared__ TLayout lay[TS_MAXL];
   __shared__ uint64_t offh[NIT];
   __shared__ int16_t nv[TS_MAXG];   // values per gate, then their offsets
@@ -1117,6 +1200,23 @@ __device__ __forceinline__ void fused_reg_body(const Cx<R>* in, Cx<R>* out,
       for (int e = 0; e < 4; ++e) mats[nv[h] + e] = acc[e];
     }
   };
+  // complex128: split the resident values into exact triples; pairs are
+  // used when every value lies in the pair range (block-uniform)
+  auto to_pairs = [&]() {
+    if constexpr (kPairs) {
+      bool bad = false;
+      for (int i = tid; i < sh_total; i += T) {
+        const C m = mats[i];
+        matsd[i] = df_entry2(m.x, m.y);
+        const uint32_t e = max(df_hiword(m.x) & 0x7ff00000u,
+                               df_hiword(m.y) & 0x7ff00000u);
+        bad |= e >= ((DF_EMAX + 1) << 20);
+      }
+      bad = __syncthreads_or(bad);
+      if (tid == 0) sh_pairs = a.df != 0 && !bad;
+      __syncthreads();
+    }
+  };
   uint64_t loaded_s = t0 / tps;
   if (resident) {
     // One thread per layout walks its gates in order.
@@ -1198,6 +1298,8 @@ __device__ __forceinline__ void fused_reg_body(const Cx<R>* in, Cx<R>* out,
     }
     has_runs = __syncthreads_or(has_runs);
     load_values(loaded_s);
+    __syncthreads();
+    to_pairs();
   }
 
   auto tile_base = [&](uint64_t t) {
@@ -1228,9 +1330,11 @@ __device__ __forceinline__ void fused_reg_body(const Cx<R>* in, Cx<R>* out,
       load_values(s);
       loaded_s = s;
       __syncthreads();
+      to_pairs();
     }
     if (a.nbuf == 2 && t + 1 < t1) prefetch(t + 1, S0 + (int)((t + 1 - t0) & 1) * M);
     const uint64_t base = tile_base(t);
+    bool tile_pairs = false;  // complex128: this tile runs in pairs
 
     for (int li = 0; li < L; ++li) {
       if (L > TS_MAXL) {  // rebuild this layout's tables in slot 0
@@ -1250,52 +1354,136 @@ __device__ __forceinline__ void fused_reg_body(const Cx<R>* in, Cx<R>* out,
           if ((i >> k) & 1) x ^= sp[k];
         return x;
       };
-#pragma unroll
-      for (int i = 0; i < NR; ++i) v[i] = S[addr(i)];
-      C ts;
-      ts.x = 1;
-      ts.y = 0;
       const int first = ly.first, count = ly.count;
-      if (resident) {
-        const int ns = ly.nscal;
-        for (int gi = first; gi < first + ns; ++gi) {
-          const TOp o = ts_load_op(&ops[gi]);
-          const int hb = o.nq == 2 ? 2 : 1;
-          int fixed = ((tb & o.x) | ((base & o.a) != 0)) ? hb : 0;
-          if ((tb & o.y) | ((base & o.b) != 0)) fixed |= 1;
-          ts = cmul(ts, mats[o.moff + fixed]);
-        }
-        ts_run<R, RB>(v, ops, mats, first + ns, first + count, tb, base, ts);
-      } else {
-        for (int c0 = 0; c0 < count; c0 += TS_CHUNK) {
-          const int cnt = min(TS_CHUNK, count - c0);
-          __syncthreads();  // the previous chunk is no longer read
-          for (int j = tid; j < cnt; j += T) {
-            const FusedGate& g = gates[first + c0 + j];
-            ops[j] = ts_decode<RB>(g, 16 * j, a.layouts[li].rb);
-            const C* src = pool + g.mat + (int64_t)s * g.mat_bstride;
-            const int k = fg_nvals(g.kind, g.nq);
-            for (int e = 0; e < k; ++e) mats[16 * j + e] = src[e];
-          }
-          __syncthreads();
-          ts_run<R, RB>(v, ops, mats, 0, cnt, tb, base, ts);
-        }
-      }
-      if (!is_one(ts)) {
+      // write-back addresses: the final relabelling of register bits
+      int spw[RB];
 #pragma unroll
-        for (int i = 0; i < NR; ++i) v[i] = cmul(ts, v[i]);
-      }
-      // write-back through the final relabelling of register bits
-#pragma unroll
-      for (int k = 0; k < RB; ++k) sp[k] = ly.spw[k];
+      for (int k = 0; k < RB; ++k) spw[k] = ly.spw[k];
       const int sbw = sb ^ ly.cw;
-#pragma unroll
-      for (int i = 0; i < NR; ++i) {
+      auto waddr = [&](int i) {
         int x = sbw;
 #pragma unroll
         for (int k = 0; k < RB; ++k)
-          if ((i >> k) & 1) x ^= sp[k];
-        S[x] = v[i];
+          if ((i >> k) & 1) x ^= spw[k];
+        return x;
+      };
+      // FP64 / complex64: the layout's operations on v
+      auto run_plain = [&]() {
+        C ts;
+        ts.x = 1;
+        ts.y = 0;
+        if (resident) {
+          const int ns = ly.nscal;
+          for (int gi = first; gi < first + ns; ++gi) {
+            const TOp o = ts_load_op(&ops[gi]);
+            const int hb = o.nq == 2 ? 2 : 1;
+            int fixed = ((tb & o.x) | ((base & o.a) != 0)) ? hb : 0;
+            if ((tb & o.y) | ((base & o.b) != 0)) fixed |= 1;
+            ts = cmul(ts, mats[o.moff + fixed]);
+          }
+          ts_run<C, C, RB>(v, ops, mats, first + ns, first + count, tb, base,
+                           ts);
+        } else {
+          for (int c0 = 0; c0 < count; c0 += TS_CHUNK) {
+            const int cnt = min(TS_CHUNK, count - c0);
+            __syncthreads();  // the previous chunk is no longer read
+            for (int j = tid; j < cnt; j += T) {
+              const FusedGate& g = gates[first + c0 + j];
+              ops[j] = ts_decode<RB>(g, 16 * j, a.layouts[li].rb);
+              const C* src = pool + g.mat + (int64_t)s * g.mat_bstride;
+              const int k = fg_nvals(g.kind, g.nq);
+              for (int e = 0; e < k; ++e) mats[16 * j + e] = src[e];
+            }
+            __syncthreads();
+            ts_run<C, C, RB>(v, ops, mats, 0, cnt, tb, base, ts);
+          }
+        }
+        if (!is_one(ts)) {
+#pragma unroll
+          for (int i = 0; i < NR; ++i) v[i] = cmul(ts, v[i]);
+        }
+      };
+
+      bool pairs = false;
+      if constexpr (kPairs) pairs = resident && sh_pairs;  // block-uniform
+      if (pairs) {
+        if constexpr (kPairs) {
+          // complex128 in pairs: the tile stays in shared memory as float
+          // pairs (16 bytes, like a double2) from the first layout's read,
+          // which splits, to the last layout's write, which renormalises
+          // and joins; in between the pairs are left unnormalised
+          float4* const S4 = reinterpret_cast<float4*>(S);
+          DC w[NR];
+          if (li == 0) {
+            uint32_t mx = 0;
+#pragma unroll
+            for (int i = 0; i < NR; ++i) {
+              v[i] = S[addr(i)];
+              mx = max(mx, max(df_hiword(v[i].x) & 0x7ff00000u,
+                               df_hiword(v[i].y) & 0x7ff00000u));
+            }
+            const bool ok = mx < ((DF_EMAX + 1) << 20) &&
+                             (mx == 0 || mx >= (DF_EMIN << 20));
+            tile_pairs = __syncthreads_and(ok);
+            if (tile_pairs) {
+#pragma unroll
+              for (int i = 0; i < NR; ++i) w[i] = df_split2(v[i].x, v[i].y);
+            }
+          } else if (tile_pairs) {
+#pragma unroll
+            for (int i = 0; i < NR; ++i) {
+              const float4 q = S4[addr(i)];
+              w[i].re = DF{q.x, q.y};
+              w[i].im = DF{q.z, q.w};
+            }
+          } else {
+#pragma unroll
+            for (int i = 0; i < NR; ++i) v[i] = S[addr(i)];
+          }
+          if (tile_pairs) {
+            DC tsd;
+            tsd.re = DF{1.f, 0.f};
+            tsd.im = DF{0.f, 0.f};
+            const int ns = ly.nscal;
+            for (int gi = first; gi < first + ns; ++gi) {
+              const TOp o = ts_load_op(&ops[gi]);
+              const int hb = o.nq == 2 ? 2 : 1;
+              int fixed = ((tb & o.x) | ((base & o.a) != 0)) ? hb : 0;
+              if ((tb & o.y) | ((base & o.b) != 0)) fixed |= 1;
+              tsd = op_scal(tsd, matsd[o.moff + fixed]);
+            }
+            ts_run<DC, DEC, RB>(w, ops, matsd, first + ns, first + count, tb,
+                                base, tsd);
+            if (!is_one(tsd)) {
+#pragma unroll
+              for (int i = 0; i < NR; ++i) w[i] = op_by_scal(tsd, w[i]);
+            }
+            if (li == L - 1) {
+#pragma unroll
+              for (int i = 0; i < NR; ++i) {
+                C y;
+                y.x = df_join(df_norm(w[i].re));
+                y.y = df_join(df_norm(w[i].im));
+                S[waddr(i)] = y;
+              }
+            } else {
+#pragma unroll
+              for (int i = 0; i < NR; ++i)
+                S4[waddr(i)] = make_float4(w[i].re.hi, w[i].re.lo,
+                                           w[i].im.hi, w[i].im.lo);
+            }
+          } else {
+            run_plain();
+#pragma unroll
+            for (int i = 0; i < NR; ++i) S[waddr(i)] = v[i];
+          }
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < NR; ++i) v[i] = S[addr(i)];
+        run_plain();
+#pragma unroll
+        for (int i = 0; i < NR; ++i) S[waddr(i)] = v[i];
       }
       __syncthreads();
     }
@@ -1387,6 +1575,7 @@ int launch_reg_stage(const void* state_in, void* state_out, const void* pool,
                          227 * 1024 - static_smem);
   }
   a.nbuf = (2 * tile + (size_t)static_smem <= 227u * 1024u) ? 2 : 1;
+  a.df = sizeof(R) == 8 && gbsv::c128_arith() == GBSV_C128_PAIRS;
   const size_t smem = tile * a.nbuf;
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
@@ -1444,6 +1633,7 @@ int launch_reg_multi(const gbsv_multi_stage_t* stages, int num, int n,
       a.num_layouts = d.num_layouts;
       a.num_states = d.num_states;
       a.nbuf = nbuf;
+      a.df = sizeof(R) == 8 && gbsv::c128_arith() == GBSV_C128_PAIRS;
       for (int j = 0; j < m; ++j) {
         if (j >= a.c) a.hpos[j - a.c] = d.tile_positions[j];
         a.spos[j] = d.tile_positions[j];

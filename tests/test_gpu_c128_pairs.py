@@ -192,3 +192,41 @@ def test_mode_round_trip(arith):
     assert ug.complex128_arithmetic() == "pairs"
     with pytest.raises(ValueError):
         ug.set_complex128_arithmetic("fp32")
+
+
+@pytest.mark.parametrize("mode", ["pairs", "fp64"])
+def test_fused_circuit_in_both_modes(oracle, arith, mode):
+    """1,000 random gates through fused register stages (14 qubits, two
+    states): within 1e-12 of the oracle and the norm within 1e-12."""
+    from qcware_unitair_gb300 import states as S
+    from qcware_unitair_gb300.circuits import random_circuit, random_states
+    from qcware_unitair_gb300.fusion import Circuit
+    arith(mode)
+    n = 14
+    gates = random_circuit(n, 1000, seed=7)
+    prog = Circuit.from_gates(n, gates).compile(torch.complex128, DEV)
+    psi0 = random_states(n, (2,), torch.complex128, seed=7)
+    out = prog.run(psi0.to(DEV))
+    ref = oracle.run_circuit([(g.matrix(), g.qubits) for g in gates],
+                             psi0.numpy())
+    err = float(np.abs(out.cpu().numpy() - ref).max())
+    drift = float((S.norm_squared_fp64(out) - 1).abs().max())
+    print(f"{mode}: passes={prog.num_passes} max|err| {err:.2e} "
+          f"drift {drift:.2e}")
+    assert err <= 1e-12
+    assert drift <= 1e-12
+
+
+def test_fused_pairs_match_fp64(arith):
+    """The same fused program in both modes agrees to pair precision."""
+    from qcware_unitair_gb300.circuits import random_circuit, random_states
+    from qcware_unitair_gb300.fusion import Circuit
+    n = 16
+    gates = random_circuit(n, 300, seed=8)
+    prog = Circuit.from_gates(n, gates).compile(torch.complex128, DEV)
+    psi0 = random_states(n, (1,), torch.complex128, seed=8).to(DEV)
+    arith("pairs")
+    a = prog.run(psi0).cpu().numpy()
+    arith("fp64")
+    b = prog.run(psi0).cpu().numpy()
+    assert float(np.abs(a - b).max()) <= 1e-13
