@@ -996,6 +996,18 @@ def run_gpu(args, ws, rank, local):
 
     e2e_step()
     torch.cuda.synchronize()
+    # the box's own pinned host-to-device rate for this buffer (untimed):
+    # it varies from box to box (23-211 GB/s seen for 8 GiB) and bounds
+    # the e2e number
+    probe = torch.empty(N, dtype=torch.complex64, device=dev)
+    c0, c1 = torch.cuda.Event(enable_timing=True), \
+        torch.cuda.Event(enable_timing=True)
+    c0.record()
+    probe.copy_(host_in, non_blocking=True)
+    c1.record()
+    torch.cuda.synchronize()
+    h2d_probe_gbs = N * 8 / (c0.elapsed_time(c1) / 1e3) / 1e9
+    del probe
     barrier()
     e2e_steps = max(1, min(args.steps, 2))
     gc.collect()
@@ -1014,6 +1026,7 @@ def run_gpu(args, ws, rank, local):
                                     for ev in e2e_ev), 2)
         for i, name in enumerate(("h2d_ms", "gates_ms", "d2h_ms"))}
     e2e_parts["wall_ms"] = round(1e3 * e2e_s / e2e_steps, 2)
+    e2e_parts["h2d_copy_alone_GBs"] = round(h2d_probe_gbs, 1)
     e2e_value = bytes_per_gate * G * e2e_steps * ws / e2e_s / 1e9
     h2d = N * 8 + sum(m.numel() * 8 for m in mats_host)
     d2h = N * 8
