@@ -10,11 +10,11 @@
 //   without unitair's 2^n integer phase tensors.
 // gbsv_multi_controlled_x  swap of the target pair where every control is
 //   1: the X that unitair builds as H, multi_controlled_z, H (:786-805).
-// gbsv_sample          draws indices from |psi|^2: FP64 sums of 1024-
-//   amplitude chunks, a scan of those sums, then one warp per sample
-//   (binary search over chunks, warp scan inside the chunk); uniforms come
-//   from a counter-based hash of (seed, sample), so results do not depend on
-//   launch order.  Replaces the Categorical sampling of measure
+// gbsv_sample          draws indices from |psi|^2: one pass builds sums of
+//   amplitude groups and chunks and a prefix over the chunks, then one
+//   thread per sample searches the chunks, the chunk's groups and the
+//   group's amplitudes; uniforms come from a counter-based hash of (seed,
+//   sample), so results do not depend on launch order.  Replaces the Categorical sampling of measure
 //   (src/unitair/simulation/measurement.py:9-70).
 #include "common.cuh"
 
@@ -514,6 +514,209 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// ---- sampling, complex64 states of whole 256-amplitude chunks ---------
+// Finer tables so that a sample reads less at random: 16-amplitude groups
+// (SUB2, FP32) inside 256-amplitude chunks, so a sample reads 64 bytes of
+// group sums and 128 bytes of amplitudes (half of the 1024 / 32 layout;
+// fewer bytes read at random per sample).  The table pass scans as it
+// goes: each warp owns a contiguous segment of chunks and writes their
+// segment-local inclusive prefix LCDF (FP64) and its total; one small
+// kernel turns the totals into segment offsets.  The chunk CDF is
+// 8 bytes per 256 amplitudes (32 MB at 30 qubits), L2-resident for the
+// searches.
+constexpr int SCHUNK = 256;
+constexpr int SGROUP = 16;
+constexpr int SGROUPS = SCHUNK / SGROUP;
+// segments of the chunk table; the sample kernel keeps their offsets in
+// shared memory ((segments + 1) doubles within 48 KB)
+constexpr int STABLE_MAX_SEGS = 6016;
+
+// Warp w of the grid owns the contiguous segment of chunks [w * per,
+// (w + 1) * per) (per is a multiple of 4) and walks it in quads, keeping
+// the running prefix as it goes, so the segment's local prefix LCDF needs
+// no second pass.  Lane l loads float4 j * 32 + l of the quad, j < 16 (8 KB
+// in flight per warp): amplitudes 64 j + 2 l and + 1, so after a 3-step
+// butterfly lanes 8 q .. 8 q + 7 hold group 4 (j & 3) + q of chunk j / 4.
+__global__ void __launch_bounds__(256)
+    sample_table_c64_kernel(const float4* psi, uint64_t nchunks,
+                            uint64_t per, double* lcdf, float* subs,
+                            double* tot) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t seg = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t first = seg * per;
+  if (first >= nchunks) return;
+  const uint64_t end = first + per < nchunks ? first + per : nchunks;
+  double run = 0.0;  // lane 0: the segment's prefix so far
+  for (uint64_t c4 = first; c4 < end; c4 += 4) {
+    const float4* src = psi + c4 * (SCHUNK / 2);
+    const int nq = end - c4 < 4 ? (int)(end - c4) : 4;  // chunks here
+    float4 q[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j)
+      q[j] = j / 4 < nq ? src[j * 32 + lane] : make_float4(0, 0, 0, 0);
+    float g[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j)
+      g[j] = fmaf(q[j].x, q[j].x,
+                  fmaf(q[j].y, q[j].y, fmaf(q[j].z, q[j].z, q[j].w * q[j].w)));
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1)
+#pragma unroll
+      for (int j = 0; j < 16; ++j)
+        g[j] += __shfl_xor_sync(0xffffffffu, g[j], o);
+    const int grp = lane >> 3;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (k >= nq) break;
+      const uint64_t c = c4 + k;
+      if ((lane & 7) == 0) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          subs[c * SGROUPS + 4 * j + grp] = g[4 * k + j];
+      }
+      // the chunk sum: its 16 FP32 group sums added with error-free
+      // TwoSum (lanes 0, 8, 16, 24 hold four each), so the chunk CDF and
+      // the group sums agree
+      float hi = 0.f, lo = 0.f;
+      if ((lane & 7) == 0) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float x = g[4 * k + j];
+          const float t = hi + x;
+          const float bp = t - hi;
+          lo += (hi - (t - bp)) + (x - bp);
+          hi = t;
+        }
+      }
+#pragma unroll
+      for (int o = 8; o < 32; o <<= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+        const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+        const float t = hi + oh;
+        const float bp = t - hi;
+        lo += ol + ((hi - (t - bp)) + (oh - bp));
+        hi = t;
+      }
+      run += (double)hi + (double)lo;
+      if (lane == 0) lcdf[c] = run;
+    }
+  }
+  if (lane == 0) tot[seg] = run;
+}
+
+// Exclusive prefix of the segment totals, in place; tot[nb] = the sum.
+__global__ void __launch_bounds__(1024)
+    sample_offsets_kernel(double* tot, int nb) {
+  constexpr int PER = (STABLE_MAX_SEGS + 1023) / 1024;
+  double v[PER], s = 0.0;
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int i = threadIdx.x * PER + k;
+    v[k] = i < nb ? tot[i] : 0.0;
+    s += v[k];
+  }
+  double total;
+  double run = block_exclusive_scan(s, &total);
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int i = threadIdx.x * PER + k;
+    if (i < nb) tot[i] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == 0) tot[nb] = total;
+}
+
+// SPT samples per thread in flight at once (independent search chains).
+template <int SPT>
+__global__ void __launch_bounds__(256)
+    sample_c64_kernel(const float4* psi, const double* lcdf,
+                      const float* subs, const double* off, int nb,
+                      uint64_t per, uint64_t nchunks, uint64_t num_samples,
+                      uint64_t seed, int64_t* out) {
+  extern __shared__ double soff[];  // block offsets, then the total
+  for (int i = threadIdx.x; i <= nb; i += blockDim.x) soff[i] = off[i];
+  __syncthreads();
+  const double total = soff[nb];
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t s0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+       s0 < num_samples; s0 += nthreads * SPT) {
+    uint64_t c[SPT], lo[SPT], hi[SPT];
+    double ub[SPT];
+    bool live[SPT];
+#pragma unroll
+    for (int k = 0; k < SPT; ++k) {
+      const uint64_t sidx = s0 + k * nthreads;
+      live[k] = sidx < num_samples;
+      const uint64_t h = mix64(seed ^ mix64(sidx));
+      const double u = (double)(h >> 11) * (1.0 / 9007199254740992.0) * total;
+      // the last segment whose offset is <= u (zero-mass segments are
+      // skipped)
+      int blo = 0, bhi = nb - 1;
+      while (blo < bhi) {
+        const int mid = (blo + bhi + 1) >> 1;
+        if (soff[mid] <= u) blo = mid; else bhi = mid - 1;
+      }
+      ub[k] = u - soff[blo];
+      lo[k] = (uint64_t)blo * per;
+      hi[k] = lo[k] + per < nchunks ? lo[k] + per - 1 : nchunks - 1;
+      c[k] = lo[k];
+    }
+    // first chunk of the segment whose local prefix exceeds the rest
+    // (rounding can leave the rest above the block's total: last chunk)
+    bool busy = true;
+    while (busy) {
+      busy = false;
+#pragma unroll
+      for (int k = 0; k < SPT; ++k) {
+        if (lo[k] < hi[k]) {
+          const uint64_t mid = (lo[k] + hi[k]) >> 1;
+          if (lcdf[mid] > ub[k]) hi[k] = mid; else lo[k] = mid + 1;
+          busy = true;
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < SPT; ++k) {
+      c[k] = lo[k];
+      const uint64_t bfirst = (c[k] / per) * per;
+      const double run = c[k] > bfirst ? lcdf[c[k] - 1] : 0.0;
+      float rem = (float)(ub[k] - run);
+      // the chunk's 16 group sums: 64 contiguous bytes
+      const float4* sv = reinterpret_cast<const float4*>(subs + c[k] * SGROUPS);
+      float4 gq[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) gq[j] = sv[j];
+      Pick gp;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        gp.add(gq[j].x, 4 * j, rem);
+        gp.add(gq[j].y, 4 * j + 1, rem);
+        gp.add(gq[j].z, 4 * j + 2, rem);
+        gp.add(gq[j].w, 4 * j + 3, rem);
+      }
+      float gex;
+      int grp = gp.result(&gex);
+      if (grp < 0) grp = 0;
+      rem -= gex;
+      // the group's 16 amplitudes: 128 contiguous bytes
+      const uint64_t gbase = c[k] * SCHUNK + (uint64_t)grp * SGROUP;
+      const float4* av = psi + gbase / 2;
+      float4 aq[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) aq[j] = av[j];
+      Pick ap;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        ap.add(fmaf(aq[j].x, aq[j].x, aq[j].y * aq[j].y), 2 * j, rem);
+        ap.add(fmaf(aq[j].z, aq[j].z, aq[j].w * aq[j].w), 2 * j + 1, rem);
+      }
+      float aex;
+      const int a = ap.result(&aex);
+      if (live[k]) out[s0 + k * nthreads] = (int64_t)gbase + (a < 0 ? 0 : a);
+    }
+  }
+}
+
 static unsigned grid_for(uint64_t work) {
   uint64_t blocks = (work + 255) / 256;
   const uint64_t cap = (uint64_t)sm_count() * 32;
@@ -687,12 +890,58 @@ static uint64_t sample_chunks(int64_t dim) {
   return ((uint64_t)dim + CHUNK - 1) / CHUNK;
 }
 
+// The finer complex64 tables: block-local CDF (FP64) per 256-amplitude
+// chunk, block totals / offsets, group sums (FP32) per 16 amplitudes.
+static size_t sample2_bytes(int64_t dim) {
+  const uint64_t chunks = ((uint64_t)dim + SCHUNK - 1) / SCHUNK;
+  return (size_t)(chunks + STABLE_MAX_SEGS + 2) * sizeof(double) +
+         (size_t)chunks * SGROUPS * sizeof(float);
+}
+
 extern "C" size_t gbsv_sample_scratch_bytes(int64_t dim) {
   if (dim <= 0) return 0;
   const uint64_t chunks = sample_chunks(dim);
   // sums and CDF (FP64), group sums (FP32), scan totals
-  return (size_t)(chunks * 2 + 1024) * sizeof(double) +
-         (size_t)chunks * GROUP * sizeof(float);
+  const size_t one = (size_t)(chunks * 2 + 1024) * sizeof(double) +
+                     (size_t)chunks * GROUP * sizeof(float);
+  const size_t two = sample2_bytes(dim);
+  return one > two ? one : two;
+}
+
+static int sample_c64_fine(const void* state, int64_t dim,
+                           int64_t num_samples, uint64_t seed,
+                           int64_t* out_indices, void* scratch,
+                           cudaStream_t st) {
+  const uint64_t nchunks = (uint64_t)dim / SCHUNK;
+  // one segment per warp of one wave of the table pass
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, sample_table_c64_kernel, 256, 0);
+  if (per_sm < 1) per_sm = 1;
+  uint64_t nb = (uint64_t)sm_count() * per_sm * 8;
+  if (nb > STABLE_MAX_SEGS) nb = STABLE_MAX_SEGS;
+  if (nb > (nchunks + 3) / 4) nb = (nchunks + 3) / 4;
+  const uint64_t per = ((nchunks + nb - 1) / nb + 3) & ~uint64_t(3);
+  nb = (nchunks + per - 1) / per;
+  double* lcdf = static_cast<double*>(scratch);
+  double* tot = lcdf + nchunks;  // nb totals, then the sum
+  float* subs = reinterpret_cast<float*>(tot + STABLE_MAX_SEGS + 2);
+  sample_table_c64_kernel<<<(unsigned)((nb + 7) / 8), 256, 0, st>>>(
+      static_cast<const float4*>(state), nchunks, per, lcdf, subs, tot);
+  int rc = after_launch("sample_table_c64_kernel");
+  if (rc) return rc;
+  sample_offsets_kernel<<<1, 1024, 0, st>>>(tot, (int)nb);
+  rc = after_launch("sample_offsets_kernel");
+  if (rc) return rc;
+  constexpr int SPT = 4;
+  uint64_t blocks = ((uint64_t)num_samples + 256 * SPT - 1) / (256 * SPT);
+  const uint64_t cap = (uint64_t)sm_count() * 8;
+  if (blocks > cap) blocks = cap;
+  const size_t smem = (nb + 1) * sizeof(double);
+  sample_c64_kernel<SPT><<<(unsigned)blocks, 256, smem, st>>>(
+      static_cast<const float4*>(state), lcdf, subs, tot, (int)nb, per,
+      nchunks, (uint64_t)num_samples, seed, out_indices);
+  return after_launch("sample_c64_kernel");
 }
 
 extern "C" int gbsv_sample(const void* state, int dtype, int64_t dim,
@@ -719,6 +968,10 @@ extern "C" int gbsv_sample(const void* state, int dtype, int64_t dim,
                      "state and scratch must be 16-byte aligned");
   if (chunks > 0x7fffffffull)
     return set_error(GBSV_ERR_UNSUPPORTED, "state too large");
+  cudaStream_t st0 = static_cast<cudaStream_t>(stream);
+  if (dtype == GBSV_C64 && dim % SCHUNK == 0)
+    return sample_c64_fine(state, dim, num_samples, seed, out_indices,
+                           scratch, st0);
   double* sums = static_cast<double*>(scratch);
   double* cdf = sums + chunks;
   double* tot = cdf + chunks;

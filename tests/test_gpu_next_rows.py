@@ -109,11 +109,36 @@ def test_measure_large_state_chunks():
     assert abs(frac - 0.36) < 0.01
 
 
+def test_measure_sparse_blocks():
+    """Mass in a few 256-amplitude chunks only (the first chunk, one in the
+    middle and the last), so most blocks of the sampling table hold zero
+    probability and the block search must skip them."""
+    n = 20
+    rng = np.random.default_rng(11)
+    amps = np.zeros(2 ** n, dtype=np.complex128)
+    for start in (0, 2 ** 19 + 3 * 256, 2 ** n - 256):
+        amps[start:start + 256] = rng.normal(size=256) + \
+            1j * rng.normal(size=256)
+    amps[::5] = 0
+    amps /= np.linalg.norm(amps)
+    st = cu(amps.astype(np.complex64))
+    N = 300000
+    idx = ug.measurement.sample(st, N, seed=21).cpu().numpy()
+    p = np.abs(amps) ** 2
+    assert np.all(p[idx] > 0)
+    support = np.flatnonzero(p)
+    freq = np.bincount(idx, minlength=2 ** n)[support] / N
+    ps = p[support]
+    sigma = np.sqrt(ps * (1 - ps) / N) + 1e-12
+    assert np.all(np.abs(freq - ps) <= 6 * sigma + 1e-9)
+
+
 @pytest.mark.parametrize("n", [1, 3, 6, 12, 16])
 @pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
 def test_measure_distribution_sizes(n, dtype):
-    """Chunks of 1024 and groups of 32 amplitudes, partial groups for tiny
-    states, zero-probability groups, both precisions."""
+    """Chunks and groups of amplitudes (256 / 16 for complex64 states of
+    whole chunks, 1024 / 32 otherwise), partial groups for tiny states,
+    zero-probability groups, both precisions."""
     rng = np.random.default_rng(n)
     amps = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
     if n >= 6:
