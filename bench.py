@@ -869,12 +869,17 @@ def wl_kinds(n: int = 28, mode: str = "pairs") -> None:
              ("T", [5]), ("Z", [5]), ("Y", [5]), ("S", [5]), ("U2", [5]),
              ("CNOT", [3, 20]), ("CZ", [3, 20]), ("SWAP", [3, 20]),
              ("CRY", [3, 20]), ("U4", [3, 20]), ("X", [n - 1]),
-             ("RX", [n - 1]), ("CNOT", [n - 2, n - 1])]
+             ("RX", [n - 1]), ("CNOT", [n - 2, n - 1]),
+             ("U8", [3, 11, 20]), ("U16", [2, 9, 15, 22])]
     for name, q in cases:
         if name == "U2":
             mat = unitary(1)
         elif name == "U4":
             mat = unitary(2)
+        elif name == "U8":
+            mat = unitary(3)
+        elif name == "U16":
+            mat = unitary(4)
         elif name == "CRY":
             mat = cry
         else:

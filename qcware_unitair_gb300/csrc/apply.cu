@@ -866,6 +866,7 @@ struct GenericArgs {
   int64_t op_stride;
   uint64_t tmask;       // bits of the target positions
   int pos[GBSV_MAX_DENSE_QUBITS];  // position of matrix bit (k-1-j)
+  int df;               // complex128: double-float pairs (1) or FP64 (0)
 };
 
 template <typename R>
@@ -933,13 +934,67 @@ __global__ void __launch_bounds__(128)
     for (int j = 0; j < K; ++j) spos[j] = p[j];
   }
   const bool shared_op = a.op_stride == 0;
+  // complex128 in pairs: the entries as exact triples, and whether all of
+  // them lie in the pair range (block-uniform)
+  constexpr bool kC128 = sizeof(R) == 8;
+  __shared__ DEC msd[kC128 ? D * D : 1];
+  bool bad = false;
   if (shared_op)
-    for (int i = tid; i < D * D; i += blockDim.x) msm[i] = ops[i];
-  __syncthreads();
+    for (int i = tid; i < D * D; i += blockDim.x) {
+      const C mv = ops[i];
+      msm[i] = mv;
+      if constexpr (kC128) {
+        msd[i] = df_entry2(mv.x, mv.y);
+        bad |= max(df_hiword(mv.x) & 0x7ff00000u,
+                   df_hiword(mv.y) & 0x7ff00000u) >= ((DF_EMAX + 1) << 20);
+      }
+    }
+  bad = __syncthreads_or(bad);
   const int n = a.n;
   const uint64_t gps = uint64_t(1) << (n - K);  // groups per state
   const uint64_t total = (a.total >> n) * gps;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  if constexpr (kC128) {
+    // one group per thread: the amplitudes split into pairs, each output
+    // a compensated dot product (df_rowD); a thread whose amplitudes leave
+    // the pair range runs the FP64 rows
+    if (shared_op && a.df && !bad) {
+      for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + tid; g < total;
+           g += stride) {
+        const uint64_t s = g / gps;
+        uint64_t base = g % gps;
+#pragma unroll
+        for (int j = 0; j < K; ++j) base = insert_zero(base, spos[j]);
+        const C* src = in + s * a.in_stride + base;
+        C* dst = out + (s << n) + base;
+        C x[D];
+#pragma unroll
+        for (int b = 0; b < D; ++b) x[b] = src[offs[b]];
+        if (pairs_in_range<C, D>(x)) {
+          DC xs[D];
+#pragma unroll
+          for (int b = 0; b < D; ++b) xs[b] = df_split2(x[b].x, x[b].y);
+#pragma unroll 2
+          for (int r = 0; r < D; ++r) {
+            const DC y = df_rowD<D>(msd + r * D, xs);
+            C o;
+            o.x = df_join(y.re);
+            o.y = df_join(y.im);
+            dst[offs[r]] = o;
+          }
+        } else {
+#pragma unroll 2
+          for (int r = 0; r < D; ++r) {
+            C acc = czero<C>();
+#pragma unroll
+            for (int b = 0; b < D; ++b) acc = cmad(msm[r * D + b], x[b], acc);
+            dst[offs[r]] = acc;
+          }
+        }
+      }
+      return;
+    }
+  }
   auto group_base = [&](uint64_t g, const C** src, C** dst) {
     const uint64_t s = g / gps;
     uint64_t base = g % gps;
@@ -1176,6 +1231,7 @@ static int apply_generic(const void* in, void* out, int dtype, int n,
   a.total = (uint64_t)num_states << n;
   a.n = n;
   a.k = k;
+  a.df = c128_arith() == GBSV_C128_PAIRS;
   a.in_stride = in_stride;
   a.op_stride = op_stride;
   for (int j = 0; j < k; ++j) {

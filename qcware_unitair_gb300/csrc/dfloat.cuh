@@ -422,4 +422,35 @@ GBSV_HD DC df_row4(const DEC* m, const DC* a) {
   return y;
 }
 
+// sum_b m_b x_b over D complex terms (one row of a D x D operator): a
+// compensated dot product (the leading parts summed with TwoSum, their
+// errors and the products' error words summed beside them, as in Ogita,
+// Rump and Oishi's Dot2), renormalised once at the end.
+template <int D>
+GBSV_HD DC df_rowD(const DEC* m, const DC* x) {
+  float sr = 0.f, er = 0.f, si = 0.f, ei = 0.f;
+#ifdef __CUDA_ARCH__
+#pragma unroll
+#endif
+  for (int b = 0; b < D; ++b) {
+    const DFP rr = df_prod(m[b].re, x[b].re);
+    const DFP ii = df_neg(df_prod(m[b].im, x[b].im));
+    const DFP ri = df_prod(m[b].re, x[b].im);
+    const DFP ir = df_prod(m[b].im, x[b].re);
+    float t;
+    sr = df_two_sum(sr, rr.p, t);
+    er = df_add_rn(er, df_add_rn(t, rr.e));
+    sr = df_two_sum(sr, ii.p, t);
+    er = df_add_rn(er, df_add_rn(t, ii.e));
+    si = df_two_sum(si, ri.p, t);
+    ei = df_add_rn(ei, df_add_rn(t, ri.e));
+    si = df_two_sum(si, ir.p, t);
+    ei = df_add_rn(ei, df_add_rn(t, ir.e));
+  }
+  DC y;
+  y.re = df_norm(DF{sr, er});
+  y.im = df_norm(DF{si, ei});
+  return y;
+}
+
 }  // namespace gbsv

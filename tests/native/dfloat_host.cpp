@@ -84,4 +84,18 @@ void dfh_gate4(const double* m, const double* a, double* y) {
   }
 }
 
+// y = M a for an 8x8 complex matrix (k = 3) through df_rowD<8>.
+void dfh_gate8(const double* m, const double* a, double* y) {
+  DC av[8];
+  for (int j = 0; j < 8; ++j) av[j] = df_split2(a[2 * j], a[2 * j + 1]);
+  for (int row = 0; row < 8; ++row) {
+    DEC e[8];
+    for (int j = 0; j < 8; ++j)
+      e[j] = df_entry2(m[16 * row + 2 * j], m[16 * row + 2 * j + 1]);
+    const DC r = df_rowD<8>(e, av);
+    y[2 * row] = df_join(r.re);
+    y[2 * row + 1] = df_join(r.im);
+  }
+}
+
 }  // extern "C"

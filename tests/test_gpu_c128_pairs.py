@@ -230,3 +230,64 @@ def test_fused_pairs_match_fp64(arith):
     arith("fp64")
     b = prog.run(psi0).cpu().numpy()
     assert float(np.abs(a - b).max()) <= 1e-13
+
+
+@pytest.mark.parametrize("mode", ["pairs", "fp64"])
+@pytest.mark.parametrize("name,qubits", [("U", [2]), ("H", [7]),
+                                         ("U4", [1, 6]), ("CRY", [7, 0])])
+def test_in_place_matches_functional(arith, mode, name, qubits):
+    """apply_operator_ (in place, the streaming kernel reading and writing
+    one buffer) gives the same bits as the functional form."""
+    arith(mode)
+    m = OPS_1Q.get(name, OPS_2Q.get(name))
+    psi = torch.from_numpy(_state(9, 3, seed=13)).to(DEV)
+    op = torch.from_numpy(m).to(DEV)
+    want = ug.apply_operator(op, qubits, psi)
+    got = psi.clone()
+    ug.apply_operator_(op, qubits, got)
+    assert torch.equal(got, want)
+
+
+@pytest.mark.parametrize("n", [7, 8])
+@pytest.mark.parametrize("name", ["U", "H", "U4", "SWAP"])
+def test_smallest_streamed_states(oracle, arith, n, name):
+    """n = 7 is one warp step per state; every target position."""
+    arith("pairs")
+    m = OPS_1Q.get(name, OPS_2Q.get(name))
+    k = int(np.log2(m.shape[0]))
+    psi = _state(n, 2, seed=n)
+    for q0 in range(n):
+        qubits = [q0] if k == 1 else [q0, (q0 + 3) % n]
+        got = _run(m, qubits, psi)
+        ref = _apply_ref(oracle, m, qubits, psi)
+        assert float(np.abs(got - ref).max()) <= 1e-13
+
+
+def test_monomial_with_phases(oracle, arith):
+    """A permutation matrix whose entries are arbitrary phases: the
+    permutation is exact, the phases go through the pairs."""
+    ph = np.exp(1j * np.array([0.3, -1.1, 2.0, 0.7]))
+    m = np.zeros((4, 4), dtype=np.complex128)
+    for r, c in enumerate([2, 0, 3, 1]):
+        m[r, c] = ph[r]
+    for mode, tol in (("pairs", 1e-13), ("fp64", 1e-15)):
+        arith(mode)
+        psi = _state(10, 2, seed=5)
+        got = _run(m, [4, 8], psi)
+        ref = _apply_ref(oracle, m, [4, 8], psi)
+        assert float(np.abs(got - ref).max()) <= tol
+
+
+@pytest.mark.parametrize("mode,tol", [("pairs", 1e-13), ("fp64", 1e-15)])
+@pytest.mark.parametrize("k,qubits", [(3, [0, 5, 9]), (3, [10, 2, 7]),
+                                      (4, [1, 4, 8, 10]), (4, [9, 0, 6, 3])])
+def test_three_and_four_qubit_operators(oracle, arith, mode, tol, k,
+                                        qubits):
+    """The group kernel: one group per thread, each output a compensated
+    dot product of pairs (df_rowD)."""
+    arith(mode)
+    m = _unitary(k, 30 + k)
+    psi = _state(11, 2, seed=k)
+    got = _run(m, qubits, psi)
+    ref = _apply_ref(oracle, m, qubits, psi)
+    assert float(np.abs(got - ref).max()) <= tol
