@@ -200,6 +200,8 @@ __global__ void __launch_bounds__(256)
 }
 
 // ---- sampling ----------------------------------------------------------
+// complex128 states and states under 256 amplitudes (complex64 states of
+// whole 256-amplitude chunks take the finer tables further below).
 // Three tables over the state: SUB[i] = sum |psi|^2 over 32-amplitude group
 // i (FP32), SUMS[c] over 1024-amplitude chunk c (32 groups, FP64), CDF =
 // inclusive prefix of SUMS.  A sample binary-searches CDF for its chunk,
@@ -256,55 +258,6 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
     if (lane == 0) sums[c] = g;
-  }
-}
-
-// complex64 states of whole chunks: one warp per chunk with coalesced
-// loads.  Load j reads float4 j * 32 + lane (amplitudes 64 j + 2 lane and
-// + 1), so lanes 0-15 cover group 2 j and lanes 16-31 group 2 j + 1.  A
-// butterfly over the 16 lanes of each half (keep one half of the values,
-// send the other) leaves lane l with the sum of group 2 (l & 15) + (l >> 4).
-// The chunk sum adds the 32 rounded group sums with an error-free FP32
-// two-sum, so the chunk CDF and the group sums agree.
-__global__ void __launch_bounds__(256)
-    chunk_sum_c64_kernel(const float4* psi, uint64_t num_chunks,
-                         double* sums, float* subs) {
-  const int lane = threadIdx.x & 31;
-  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  for (uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-       c < num_chunks; c += nwarps) {
-    const float4* src = psi + c * (CHUNK / 2);
-    float4 q[16];
-#pragma unroll
-    for (int j = 0; j < 16; ++j) q[j] = src[j * 32 + lane];
-    float p[16];
-#pragma unroll
-    for (int j = 0; j < 16; ++j)
-      p[j] = fmaf(q[j].x, q[j].x,
-                  fmaf(q[j].y, q[j].y, fmaf(q[j].z, q[j].z, q[j].w * q[j].w)));
-#pragma unroll
-    for (int k = 8; k > 0; k >>= 1) {
-      const bool up = (lane & k) != 0;
-#pragma unroll
-      for (int i = 0; i < k; ++i) {
-        const float send = up ? p[i] : p[i + k];
-        const float keep = up ? p[i + k] : p[i];
-        p[i] = keep + __shfl_xor_sync(0xffffffffu, send, k);
-      }
-    }
-    const float g = p[0];
-    subs[c * GROUP + 2 * (lane & 15) + (lane >> 4)] = g;
-    float hi = g, lo = 0.f;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
-      const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
-      const float t = hi + oh;
-      const float bp = t - hi;
-      lo += ol + ((hi - (t - bp)) + (oh - bp));
-      hi = t;
-    }
-    if (lane == 0) sums[c] = (double)hi + (double)lo;
   }
 }
 
@@ -956,11 +909,18 @@ static uint64_t sample_chunks(int64_t dim) {
   return ((uint64_t)dim + CHUNK - 1) / CHUNK;
 }
 
-// The finer complex64 tables: block-local CDF (FP64) per 256-amplitude
-// chunk, block totals / offsets, group sums (FP32) per 16 amplitudes.
+// The finer complex64 tables: segment-local chunk prefix (FP64) per
+// 256-amplitude chunk, segment totals / offsets, group sums (FP32) per 16
+// amplitudes.  Doubles before the group sums: the chunk prefix, the segment totals and
+// their sum, rounded up to an even count so that the group sums start on
+// a 16-byte boundary (they are read as float4).
+static uint64_t sample2_doubles(uint64_t chunks) {
+  return (chunks + STABLE_MAX_SEGS + 2 + 1) & ~uint64_t(1);
+}
+
 static size_t sample2_bytes(int64_t dim) {
   const uint64_t chunks = ((uint64_t)dim + SCHUNK - 1) / SCHUNK;
-  return (size_t)(chunks + STABLE_MAX_SEGS + 2) * sizeof(double) +
+  return (size_t)sample2_doubles(chunks) * sizeof(double) +
          (size_t)chunks * SGROUPS * sizeof(float);
 }
 
@@ -991,7 +951,7 @@ static int sample_c64_fine(const void* state, int64_t dim,
   nb = (nchunks + per - 1) / per;
   double* lcdf = static_cast<double*>(scratch);
   double* tot = lcdf + nchunks;  // nb totals, then the sum
-  float* subs = reinterpret_cast<float*>(tot + STABLE_MAX_SEGS + 2);
+  float* subs = reinterpret_cast<float*>(lcdf + sample2_doubles(nchunks));
   sample_table_c64_kernel<<<(unsigned)((nb + 7) / 8), 256, 0, st>>>(
       static_cast<const float4*>(state), nchunks, per, lcdf, subs, tot);
   int rc = after_launch("sample_table_c64_kernel");
@@ -1047,10 +1007,7 @@ extern "C" int gbsv_sample(const void* state, int dtype, int64_t dim,
     uint64_t blocks = (chunks * 32 + 255) / 256;
     const uint64_t cap = (uint64_t)sm_count() * 16;
     if (blocks > cap) blocks = cap;
-    if (dtype == GBSV_C64 && dim % CHUNK == 0)
-      chunk_sum_c64_kernel<<<(unsigned)blocks, 256, 0, st>>>(
-          static_cast<const float4*>(state), chunks, sums, subs);
-    else if (dtype == GBSV_C64)
+    if (dtype == GBSV_C64)
       chunk_sum_kernel<float><<<(unsigned)blocks, 256, 0, st>>>(
           static_cast<const float2*>(state), chunks, (uint64_t)dim, sums, subs);
     else

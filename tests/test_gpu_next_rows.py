@@ -133,7 +133,7 @@ def test_measure_sparse_blocks():
     assert np.all(np.abs(freq - ps) <= 6 * sigma + 1e-9)
 
 
-@pytest.mark.parametrize("n", [1, 3, 6, 12, 16])
+@pytest.mark.parametrize("n", [1, 3, 6, 8, 9, 12, 16])
 @pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
 def test_measure_distribution_sizes(n, dtype):
     """Chunks and groups of amplitudes (256 / 16 for complex64 states of
@@ -234,3 +234,4 @@ def test_tensor_layout_variants(dtype):
     assert torch.equal(got,
                        ug.simulation.permute_qubits_tensor(perm, T, n)
                        .contiguous())
+
