@@ -75,3 +75,25 @@ def test_engine_refuses_cpu_tensors():
                           torch.ones(4, dtype=torch.complex64))
     with pytest.raises(RuntimeError, match="CUDA"):
         ug.norm_squared(torch.ones(4, dtype=torch.complex64))
+
+
+def test_complex128_arithmetic_switch_without_gpu(lib_built):
+    """gbsv_set_c128_arith / gbsv_get_c128_arith: both modes round-trip, an
+    unknown mode is rejected and leaves the setting alone; no device call."""
+    L = _lib.load()
+    prev = L.gbsv_get_c128_arith()
+    try:
+        assert L.gbsv_set_c128_arith(1) == 0
+        assert L.gbsv_get_c128_arith() == 1
+        assert L.gbsv_set_c128_arith(0) == 0
+        assert L.gbsv_get_c128_arith() == 0
+        assert L.gbsv_set_c128_arith(7) == _lib.GBSV_ERR_INVALID_ARG
+        assert b"unknown complex128 arithmetic mode" in L.gbsv_last_error()
+        assert L.gbsv_get_c128_arith() == 0
+        import qcware_unitair_gb300 as ug
+        assert ug.set_complex128_arithmetic("fp64") == "pairs"
+        assert ug.complex128_arithmetic() == "fp64"
+        with pytest.raises(ValueError):
+            ug.set_complex128_arithmetic("double")
+    finally:
+        L.gbsv_set_c128_arith(prev)
