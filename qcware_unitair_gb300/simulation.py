@@ -147,16 +147,22 @@ def _dagger(ops: torch.Tensor) -> torch.Tensor:
     return ops.conj().transpose(-1, -2).contiguous()
 
 
+def _apply_forward(operator, state, qubits, n, k):
+    """The forward launch; returns (out, plan, contiguous state)."""
+    plan = _BatchPlan(operator, state, n, k)
+    state_c = state.contiguous()
+    out = torch.empty(plan.out_batch + (2 ** n,), dtype=state.dtype,
+                      device=state.device)
+    if plan.num_states:
+        _launch_apply(plan.ops, plan.op_stride, state_c, plan.in_stride,
+                      out, n, qubits, plan.num_states)
+    return out, plan, state_c
+
+
 class _ApplyOperator(torch.autograd.Function):
     @staticmethod
     def forward(ctx, operator, state, qubits, n, k):
-        plan = _BatchPlan(operator, state, n, k)
-        state_c = state.contiguous()
-        out = torch.empty(plan.out_batch + (2 ** n,), dtype=state.dtype,
-                          device=state.device)
-        if plan.num_states:
-            _launch_apply(plan.ops, plan.op_stride, state_c, plan.in_stride,
-                          out, n, qubits, plan.num_states)
+        out, plan, state_c = _apply_forward(operator, state, qubits, n, k)
         ctx.qubits, ctx.n, ctx.k = qubits, n, k
         ctx.plan = plan
         ctx.op_shape = operator.shape
@@ -221,7 +227,12 @@ def apply_operator(operator: torch.Tensor, qubits: Iterable[int],
     contiguous tensor; differentiable with respect to both inputs.
     """
     n, qubits, k = _validate_apply(operator, qubits, state)
-    return _ApplyOperator.apply(operator, state, tuple(qubits), n, k)
+    if torch.is_grad_enabled() and (operator.requires_grad or
+                                    state.requires_grad):
+        return _ApplyOperator.apply(operator, state, tuple(qubits), n, k)
+    # no gradient can flow: the same launch without the autograd Function
+    # (its bookkeeping is most of a small state's per-gate host time)
+    return _apply_forward(operator, state, qubits, n, k)[0]
 
 
 def apply_operator_(operator: torch.Tensor, qubits: Iterable[int],
