@@ -900,6 +900,25 @@ def wl_kinds(n: int = 28, mode: str = "pairs") -> None:
               f"{2 * 16 * 2 ** n / ms / 1e6:.0f} GB/s")
 
 
+def wl_phase128(n: int = 28) -> None:
+    """apply_phase on an n-qubit complex128 state with float64 angles, in
+    both complex128 arithmetic modes."""
+    import torch
+    import qcware_unitair_gb300 as ug
+    dev = torch.device("cuda")
+    g = torch.Generator(device=dev)
+    g.manual_seed(0)
+    psi = torch.randn(2 ** n, dtype=torch.complex128, device=dev, generator=g)
+    ang = torch.rand(2 ** n, dtype=torch.float64, device=dev,
+                     generator=g) * 6.3
+    for mode in ("pairs", "fp64"):
+        ug.set_complex128_arithmetic(mode)
+        ms = _wl_timed(lambda: ug.apply_phase(ang, psi))
+        gbs = 2 ** n * (16 + 16 + 8) / ms / 1e6
+        print(f"phase128 n={n} {mode}: {ms:.3f} ms {gbs:.0f} GB/s")
+    ug.set_complex128_arithmetic("pairs")
+
+
 def run_workload(argv):
     import torch  # noqa: F401  (CUDA initialised before the workload)
     what, args = argv[0], argv[1:]
@@ -920,6 +939,8 @@ def run_workload(argv):
         wl_adjoint(*(int(a) for a in args))
     elif what == "serve":
         wl_serve(*(int(a) for a in args))
+    elif what == "phase128":
+        wl_phase128(int(args[0]) if args else 28)
     elif what == "kinds":
         wl_kinds(int(args[0]) if args else 28,
                  args[1] if len(args) > 1 else "pairs")

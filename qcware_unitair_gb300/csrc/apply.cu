@@ -1379,14 +1379,42 @@ struct PhaseArgs {
   int64_t shape[GBSV_MAX_DIMS];
   int64_t sa[GBSV_MAX_DIMS];
   int64_t sb[GBSV_MAX_DIMS];
+  int df;  // double angles: double-float pairs (1) or FP64 (0)
 };
 
 // out = (cos t - i sin t) * psi.
 template <typename RA, typename RS, typename RO>
-__device__ __forceinline__ Cx<RO> phase_one(RA t, Cx<RS> v) {
+__device__ __forceinline__ Cx<RO> phase_one(RA t, Cx<RS> v, int df) {
   // The phase factor is formed in the angle's precision, as torch forms
   // exp(-1j * angles) in complex(angles.dtype); the product is then taken
   // in the promoted output precision.
+  if constexpr (sizeof(RA) == 8) {
+    // double angles in pairs (df_sincos) when the angle is within 2^20 and
+    // the amplitude within the pair range; FP64 otherwise
+    uint32_t mx = 0;
+    if constexpr (sizeof(RS) == 8)
+      mx = max(df_hiword(v.x) & 0x7ff00000u, df_hiword(v.y) & 0x7ff00000u);
+    const bool ok = df && (df_hiword(t) & 0x7ff00000u) <= ((1023u + 19) << 20) &&
+                    (sizeof(RS) == 4 ||
+                     (mx < ((DF_EMAX + 1) << 20) &&
+                      (mx == 0 || mx >= (DF_EMIN << 20))));
+    if (ok) {
+      const DSC sc = df_sincos(t);
+      DC a;
+      if constexpr (sizeof(RS) == 8) {
+        a = df_split2(v.x, v.y);
+      } else {
+        a.re = DF{(float)v.x, 0.f};
+        a.im = DF{(float)v.y, 0.f};
+      }
+      const DF re = df_sum2(df_prod2(sc.c, a.re), df_prod2(sc.s, a.im));
+      const DF im = df_sum2(df_prod2(sc.c, a.im), df_neg(df_prod2(sc.s, a.re)));
+      Cx<RO> o;
+      o.x = df_join(re);
+      o.y = df_join(im);
+      return o;
+    }
+  }
   RA sa, ca;
   sincos(t, &sa, &ca);
   const RO s = (RO)sa, c = (RO)ca;
@@ -1415,7 +1443,7 @@ __global__ void __launch_bounds__(256)
       }
 #pragma unroll
       for (int k = 0; k < 4; ++k)
-        out[i + k * stride] = phase_one<RA, RS, RO>(t[k], v[k]);
+        out[i + k * stride] = phase_one<RA, RS, RO>(t[k], v[k], a.df);
     }
   }
   for (; i < a.total; i += stride) {
@@ -1433,7 +1461,7 @@ __global__ void __launch_bounds__(256)
         ob += (int64_t)idx * a.sb[d];
       }
     }
-    out[i] = phase_one<RA, RS, RO>(ang[oa], psi[ob]);
+    out[i] = phase_one<RA, RS, RO>(ang[oa], psi[ob], a.df);
   }
 }
 
@@ -1474,6 +1502,7 @@ extern "C" int gbsv_apply_phase(const void* angles, int angle_dtype,
                      "output dtype %d is not the promoted type %d", out_dtype,
                      want);
   PhaseArgs a{};
+  a.df = c128_arith() == GBSV_C128_PAIRS;
   a.ndim = bc->ndim;
   uint64_t total = 1;
   for (int d = 0; d < bc->ndim; ++d) {

@@ -453,4 +453,112 @@ GBSV_HD DC df_rowD(const DEC* m, const DC* x) {
   return y;
 }
 
+// ---- sine and cosine in pairs --------------------------------------------
+// sin and cos of a double angle with |theta| <= 2^20, as pairs, written
+// from the mathematics: Cody and Waite's reduction theta = k pi/2 + r with
+// pi/2 held as three floats C1 + C2 + C3 (72 bits; each k Ci taken exactly
+// by fma, theta.hi - k C1 exact by Sterbenz's lemma for k != 0, the other
+// parts summed with TwoSum and their errors kept beside), then the Taylor
+// series of sin and cos on |r| <= pi/4 (plus a rounding margin): the
+// coefficients 1/n! whose terms exceed about 2^-25 of the result as pairs,
+// the remaining tail in FP32.  The constants are the floats nearest to
+// pi/2's parts, 2/pi and the pair splits of (-1)^j / n!, computed from
+// exact rationals.
+struct DSC {
+  DF s, c;
+};
+
+GBSV_HD float df_rint(float x) {
+#ifdef __CUDA_ARCH__
+  return rintf(x);
+#else
+  return nearbyintf(x);
+#endif
+}
+
+// a * b for two pairs: the leading product exactly, the cross terms into
+// the error word
+GBSV_HD DFP df_prod2(DF a, DF b) {
+  DFP r;
+  r.p = df_mul_rn(a.hi, b.hi);
+  float e = df_fma(a.hi, b.hi, -r.p);
+  e = df_fma(a.hi, b.lo, e);
+  e = df_fma(a.lo, b.hi, e);
+  r.e = e;
+  return r;
+}
+// a * b + c, renormalised
+GBSV_HD DF df_mad2(DF a, DF b, DF c) {
+  const DFP p = df_prod2(a, b);
+  float es;
+  const float s = df_two_sum(p.p, c.hi, es);
+  return df_fast2(s, df_add_rn(es, df_add_rn(p.e, c.lo)));
+}
+
+GBSV_HD DSC df_sincos(double theta) {
+  constexpr float PIO2_1 = 0x1.921fb6p+0f, PIO2_2 = -0x1.777a5cp-25f,
+                  PIO2_3 = -0x1.ee59dap-50f, TWO_OVER_PI = 0x1.45f306p-1f;
+  // sin r = r + r z S(z), z = r^2: S0..S3 as pairs, S4..S7 in FP32
+  const DF S0{-0x1.555556p-3f, 0x1.555556p-28f};
+  const DF S1{0x1.111112p-7f, -0x1.dddddep-32f};
+  const DF S2{-0x1.a01a02p-13f, 0x1.7f97fap-39f};
+  const DF S3{0x1.71de3ap-19f, 0x1.55b1ccp-45f};
+  constexpr float S4 = -0x1.ae6456p-26f, S5 = 0x1.612462p-33f,
+                  S6 = -0x1.ae7f3ep-41f, S7 = 0x1.952c78p-49f;
+  // cos r = 1 + z C(z): C0..C4 as pairs, C5..C8 in FP32
+  const DF C0{-0.5f, 0.f};
+  const DF C1{0x1.555556p-5f, -0x1.555556p-30f};
+  const DF C2{-0x1.6c16c2p-10f, 0x1.27d27ep-35f};
+  const DF C3{0x1.a01a02p-16f, -0x1.7f97fap-42f};
+  const DF C4{-0x1.27e4fcp-22f, 0x1.10ec14p-47f};
+  constexpr float C5 = 0x1.1eed8ep-29f, C6 = -0x1.93974ap-37f,
+                  C7 = 0x1.ae7f3ep-45f, C8 = -0x1.682786p-53f;
+
+  const DE t = df_entry(theta);
+  const float kf = df_rint(df_mul_rn(t.hi, TWO_OVER_PI));
+  const float p1 = df_mul_rn(kf, PIO2_1), e1 = df_fma(kf, PIO2_1, -p1);
+  const float p2 = df_mul_rn(kf, PIO2_2), e2 = df_fma(kf, PIO2_2, -p2);
+  const float p3 = df_mul_rn(kf, PIO2_3);
+  float s = df_sub_rn(t.hi, p1);
+  float q, err;
+  s = df_two_sum(s, -e1, err);
+  s = df_two_sum(s, t.mid, q);
+  err = df_add_rn(err, q);
+  s = df_two_sum(s, -p2, q);
+  err = df_add_rn(err, q);
+  err = df_add_rn(err, df_sub_rn(df_sub_rn(t.lo, e2), p3));
+  const DF r = df_fast2(s, err);
+  const DFP zp = df_prod2(r, r);
+  const DF z = df_fast2(zp.p, zp.e);
+
+  float ts = df_fma(z.hi, S7, S6);
+  ts = df_fma(z.hi, ts, S5);
+  ts = df_fma(z.hi, ts, S4);
+  DF as = df_mad2(z, DF{ts, 0.f}, S3);
+  as = df_mad2(z, as, S2);
+  as = df_mad2(z, as, S1);
+  as = df_mad2(z, as, S0);
+  const DFP wp = df_prod2(z, as);
+  const DF sr = df_mad2(r, df_fast2(wp.p, wp.e), r);
+
+  float tc = df_fma(z.hi, C8, C7);
+  tc = df_fma(z.hi, tc, C6);
+  tc = df_fma(z.hi, tc, C5);
+  DF ac = df_mad2(z, DF{tc, 0.f}, C4);
+  ac = df_mad2(z, ac, C3);
+  ac = df_mad2(z, ac, C2);
+  ac = df_mad2(z, ac, C1);
+  ac = df_mad2(z, ac, C0);
+  const DF cr = df_mad2(z, ac, DF{1.f, 0.f});
+
+  // quadrant k mod 4
+  const int quad = ((int)kf) & 3;
+  DSC o;
+  o.s = (quad & 1) ? cr : sr;
+  o.c = (quad & 1) ? sr : cr;
+  if (quad == 2 || quad == 3) o.s = df_neg(o.s);
+  if (quad == 1 || quad == 2) o.c = df_neg(o.c);
+  return o;
+}
+
 }  // namespace gbsv

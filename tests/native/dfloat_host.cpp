@@ -98,4 +98,10 @@ void dfh_gate8(const double* m, const double* a, double* y) {
   }
 }
 
+void dfh_sincos(double theta, double* out) {
+  const DSC r = df_sincos(theta);
+  out[0] = df_join(r.s);
+  out[1] = df_join(r.c);
+}
+
 }  // extern "C"

@@ -291,3 +291,37 @@ def test_three_and_four_qubit_operators(oracle, arith, mode, tol, k,
     got = _run(m, qubits, psi)
     ref = _apply_ref(oracle, m, qubits, psi)
     assert float(np.abs(got - ref).max()) <= tol
+
+
+@pytest.mark.parametrize("mode,tol", [("pairs", 2e-14), ("fp64", 1e-15)])
+@pytest.mark.parametrize("scale", [1.0, 100.0, 1e5])
+def test_apply_phase_double_angles(arith, mode, tol, scale):
+    """apply_phase with float64 angles: the phase factor in pairs
+    (df_sincos: Cody-Waite reduction, Taylor series) or FP64, against
+    numpy's exp(-1j * angles) * state in complex128."""
+    arith(mode)
+    n = 12
+    rng = np.random.default_rng(int(scale))
+    ang = rng.uniform(-scale, scale, size=(2, 2 ** n))
+    ang[0, :64] = np.arange(-32, 32) * (np.pi / 2)  # exact-cancellation cases
+    ang[1, :8] = [0.0, 1e-300, -1e-12, 2.0 ** 19, 3e6, -3e6, np.pi, 1e-40]
+    psi = _state(n, 2, seed=3)
+    got = ug.apply_phase(torch.from_numpy(ang).to(DEV),
+                         torch.from_numpy(psi).to(DEV)).cpu().numpy()
+    want = np.exp(-1j * ang) * psi
+    assert float(np.abs(got - want).max()) <= tol * np.abs(psi).max() * 100
+
+
+def test_apply_phase_double_angles_on_complex64(arith):
+    """float64 angles on a complex64 state: complex128 output, the phase
+    in pairs."""
+    arith("pairs")
+    n = 10
+    rng = np.random.default_rng(4)
+    ang = rng.uniform(-10, 10, size=2 ** n)
+    psi = _state(n, 1, seed=4).astype(np.complex64)
+    got = ug.apply_phase(torch.from_numpy(ang).to(DEV),
+                         torch.from_numpy(psi).to(DEV))
+    assert got.dtype == torch.complex128
+    want = np.exp(-1j * ang) * psi.astype(np.complex128)
+    assert float(np.abs(got.cpu().numpy() - want).max()) <= 1e-15
