@@ -276,3 +276,29 @@ def test_8x8_rows_vs_exact_and_unbiased(lib):
     # spread about 39 per output norm: the mean of 300 is within +-2.3 (one
     # sigma); a fixed-sign rounding shows as about -39
     assert abs(np.mean(dn)) < 10.0, np.mean(dn)
+
+
+def test_sincos_vs_high_precision(lib):
+    """df_sincos (apply_phase's phase factor for float64 angles) against
+    50-digit values: a few 2^-47 absolute at most, for angles up to 2^20,
+    multiples of pi/2 and tiny angles."""
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.dps = 50
+    d2 = ctypes.c_double * 2
+    lib.dfh_sincos.argtypes = [ctypes.c_double, d2]
+    rng = np.random.default_rng(50)
+    vals = (list(rng.uniform(-7, 7, 800)) +
+            list(rng.uniform(-2.0 ** 20, 2.0 ** 20, 800)) +
+            list(rng.uniform(-1e-3, 1e-3, 100)) +
+            [k * math.pi / 2 for k in range(-40, 41)] +
+            [0.0, 1e-30, -1e-30, 2.0 ** 20 - 1, math.pi / 4] +
+            [k * math.pi / 2 + d for k in (1, 3, 1000, 654321)
+             for d in (1e-9, -1e-9, 1e-15)])
+    worst = 0.0
+    for x in vals:
+        o = d2()
+        lib.dfh_sincos(float(x), o)
+        xs = mpmath.mpf(float(x))
+        worst = max(worst, abs(float(o[0] - mpmath.sin(xs))),
+                    abs(float(o[1] - mpmath.cos(xs))))
+    assert worst <= 2.0 ** -45, worst
