@@ -14,6 +14,12 @@
 // bit position is >= log2(V) ("high" targets) select which chunks a thread
 // loads together (2 for one high target, 4 for two); targets below log2(V)
 // ("low" targets) pair amplitudes inside a chunk, in registers.
+//
+// complex128 with one operator for every state (n >= 7) runs in
+// dense_c128_stream_kernel instead: warp steps of 128 amplitudes streamed
+// through shared memory, with the arithmetic in double-float pairs
+// (dfloat.cuh); the chunked kernel keeps complex128 per-state operators,
+// small states and unaligned views.
 #include <stdio.h>
 
 #include <algorithm>
@@ -625,7 +631,7 @@ __global__ void __launch_bounds__(256, 3)
   constexpr int NR = NCH * V;
   constexpr int D = 1 << K;
   // amplitudes per thread: complex128 keeps four so that the pair
-  // arithmetic fits about 72 registers (three blocks per SM)
+  // arithmetic fits the 85 registers of three blocks per SM
   constexpr int TARGET = sizeof(R) == 4 ? 16 : 4;
   constexpr int UNROLL = NR >= TARGET ? 1 : TARGET / NR;
   constexpr bool kC128 = sizeof(R) == 8;
