@@ -16,6 +16,8 @@
 //   group's amplitudes; uniforms come from a counter-based hash of (seed,
 //   sample), so results do not depend on launch order.  Replaces the Categorical sampling of measure
 //   (src/unitair/simulation/measurement.py:9-70).
+#include <atomic>
+
 #include "common.cuh"
 
 namespace gbsv {
@@ -939,11 +941,18 @@ static int sample_c64_fine(const void* state, int64_t dim,
                            int64_t* out_indices, void* scratch,
                            cudaStream_t st) {
   const uint64_t nchunks = (uint64_t)dim / SCHUNK;
-  // one segment per warp of one wave of the table pass
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &per_sm, sample_table_c64_kernel, 256, 0);
-  if (per_sm < 1) per_sm = 1;
+  // one segment per warp of one wave of the table pass (the occupancy
+  // query once per device: it is host work before the first launch)
+  static std::atomic<int> per_sm_of[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int per_sm = per_sm_of[dev & 63].load(std::memory_order_relaxed);
+  if (per_sm == 0) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, sample_table_c64_kernel, 256, 0);
+    if (per_sm < 1) per_sm = 1;
+    per_sm_of[dev & 63].store(per_sm, std::memory_order_relaxed);
+  }
   uint64_t nb = (uint64_t)sm_count() * per_sm * 8;
   if (nb > STABLE_MAX_SEGS) nb = STABLE_MAX_SEGS;
   if (nb > (nchunks + 3) / 4) nb = (nchunks + 3) / 4;
