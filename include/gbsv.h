@@ -101,8 +101,11 @@ int gbsv_get_c128_arith(void);
  * the permute -> einsum -> permute sequence becomes one pass that addresses
  * amplitude pairs / quads by bit insertion.  qubits is a HOST array.
  * state_in == state_out (in place) is supported for k <= 5 (complex64) /
- * k <= 4 (complex128) and k = 0; wider operators in place return
- * GBSV_ERR_UNSUPPORTED. */
+ * k <= 4 (complex128), and for complex64 operators on 6-12 qubits over
+ * contiguous states (in_stride == 2^num_qubits when num_states > 1) except
+ * per-state operators (op_stride != 0) on states of fewer than 2^(13-k)
+ * groups of 2^k amplitudes (2^7 for k = 6).  Other in-place requests
+ * return GBSV_ERR_UNSUPPORTED. */
 int gbsv_apply_operator(const void* state_in, void* state_out, int dtype,
                         int num_qubits, int64_t num_states, int64_t in_stride,
                         const void* ops, int64_t op_stride,

@@ -103,7 +103,19 @@ def broadcast_strides(t: torch.Tensor, out_shape) -> list:
             for s, st, o in zip(shape, strides, out_shape)]
 
 
-def max_inplace_qubits(dtype) -> int:
-    """Widest operator gbsv_apply_operator applies in place (state_in ==
-    state_out); wider ones go through a temporary."""
-    return 5 if dtype == torch.complex64 else 4
+def wide_group_bits(k: int) -> int:
+    """log2 of the groups of 2^k amplitudes one tile of the complex64
+    wide-operator kernel holds (k = 6..12)."""
+    return 7 if k == 6 else 13 - k
+
+
+def inplace_ok(dtype, k: int, n: int, per_state: bool = False) -> bool:
+    """Whether gbsv_apply_operator applies a k-qubit operator in place
+    (state_in == state_out) on contiguous n-qubit states; otherwise callers
+    go through a temporary.  complex64 operators on 6-12 qubits are in place
+    unless they are per-state and a state holds fewer groups than one tile
+    of the wide-operator kernel."""
+    if k <= (5 if dtype == torch.complex64 else 4):
+        return True
+    return (dtype == torch.complex64 and k <= 12 and
+            (not per_state or n - k >= wide_group_bits(k)))

@@ -399,7 +399,7 @@ def _backward_sweep(pc, params, H, psi_L, saved, dtype):
             else:
                 _, m, qs, _kind = op
                 md = dag[id(op)]
-                wide = len(qs) > _core.max_inplace_qubits(dtype)
+                wide = not _core.inplace_ok(dtype, len(qs), n)
                 dst = torch.empty_like(both) if wide else both
                 rc = L.gbsv_apply_operator(
                     both.data_ptr(), dst.data_ptr(), code, n, 2 * B, N,
@@ -662,7 +662,7 @@ def _backward_fused(pc, params, H, psi_L, saved, dtype):
             else:
                 _, m_, qs, _k = entry[1]
                 md = m_.conj().T.contiguous().to(device=dev, dtype=dtype)
-                wide = len(qs) > _core.max_inplace_qubits(dtype)
+                wide = not _core.inplace_ok(dtype, len(qs), n)
                 dst = torch.empty_like(both) if wide else both
                 rc = L.gbsv_apply_operator(
                     both.data_ptr(), dst.data_ptr(), code, n, 2 * B, N,

@@ -862,8 +862,9 @@ __global__ void __launch_bounds__(C128_THREADS, 2)
 }
 
 // Any k <= GBSV_MAX_DENSE_QUBITS: one thread per output amplitude,
-// out[i] = sum_b M[row(i), b] * in[base(i) + offs[b]].  Used for k = 0 and
-// k >= 3, where no configuration of the engine is bandwidth-critical.
+// out[i] = sum_b M[row(i), b] * in[base(i) + offs[b]].  Used for k = 0,
+// complex128 with k >= 5 and the complex64 cases dense_wide_kernel leaves
+// (per-state operators on states of fewer than one tile of groups).
 struct GenericArgs {
   uint64_t total;  // num_states << n
   int n;
@@ -1229,10 +1230,324 @@ static int apply_small(const void* in, void* out, int dtype, int n,
   return dispatch_chunk<double>(V, k, nh, rb[0], rb[1], in, out, ops, a, st);
 }
 
+// ------------------------------------------------ wide operators (c64) ----
+// k = 6..12 target qubits, complex64: a CTA holds a "tile" of BN groups (all
+// 2^k amplitudes of each, 8192 amplitudes = 64 KB) in shared memory and
+// computes the D x BN output tile as a complex matrix product, the operator
+// streamed through shared memory in chunks of BK columns (k = 6 keeps the
+// whole 64 x 64 operator resident).  Each thread accumulates TM x TN = 32
+// outputs in registers; per k-step it reads TM operator entries (two thread
+// rows per warp: broadcasts) and TN/2 16-byte amplitude pairs.  Every output
+// sums over the operator's columns in order with the fused multiply-adds of
+// dense_generic_kernel, so both kernels give the same bits.  A tile is read
+// completely before any of it is written, and tiles are disjoint, so in
+// place is safe.
+template <int K>
+struct WideCfg {
+  static constexpr int D = 1 << K;
+  static constexpr int LBN = K == 6 ? 7 : 13 - K;  // log2 groups per tile
+  static constexpr int BN = 1 << LBN;
+  static constexpr int BK = 4096 >> K;             // columns per chunk
+  static constexpr int TN = K == 6 ? 8 : (K == 12 ? 2 : 4);
+  static constexpr int TM = 32 / TN;
+  static constexpr int NTC = BN / TN;              // thread columns
+  static constexpr int NTR = 256 / NTC;            // thread rows
+  static constexpr int LDM = BK + 1;               // padded chunk row
+  static constexpr int SWM = (BN / 2 < 16 ? BN / 2 : 16) - 1;
+  static constexpr size_t SMEM = (size_t)(D * BN + D * LDM) * 8;
+  static_assert(NTR * TM == D && NTC * TN == BN && D * BN == 8192, "");
+};
+
+struct WideArgs {
+  uint64_t groups;  // num_states << (n - k)
+  int n;
+  int lgps;         // log2 groups per state (n - k)
+  int vec;          // output column pairs adjacent and 16-byte aligned
+  int nspos;
+  int64_t in_stride;
+  int64_t op_stride;
+  int spos[GBSV_MAX_DENSE_QUBITS];     // target positions, ascending
+  int64_t boff[GBSV_MAX_DENSE_QUBITS]; // address offset of matrix bit m
+  int64_t cout[7];   // output address offset of tile column bit q
+  // the 13 bits of a tile element index (row b, column c), lowest input
+  // address first: input address offset and shared index (b * BN + c)
+  int64_t ein[13];
+  int32_t eix[13];
+  int64_t rj[16];    // offs(2 * NTR * (i >> 1) + (i & 1)), i < TM
+  int64_t cj[8];     // output offset of column 2 * NTC * (j >> 1) + (j & 1)
+};
+
+template <int K>
+__global__ void __launch_bounds__(256, K <= 10 ? 2 : 1)
+    dense_wide_kernel(const float2* in, float2* out, const float2* ops,
+                      WideArgs a) {
+  using W = WideCfg<K>;
+  constexpr int D = W::D, BN = W::BN, BK = W::BK, TM = W::TM, TN = W::TN,
+                NTC = W::NTC, NTR = W::NTR, LDM = W::LDM, SWM = W::SWM;
+  constexpr bool kResident = BK == D;
+  extern __shared__ __align__(16) float2 wsm[];
+  float2* xs = wsm;           // [D][BN] the tile, columns XOR-swizzled
+  float2* ms = wsm + D * BN;  // [D][LDM] columns kc .. kc + BK - 1
+  __shared__ int64_t it_in[32];
+  __shared__ int32_t it_ix[32];
+  const int tid = threadIdx.x;
+  if (tid < 32) {  // element bits 8..12 come from the copy iteration
+    int64_t g = 0;
+    int32_t x = 0;
+    for (int j = 0; j < 5; ++j)
+      if ((tid >> j) & 1) {
+        g += a.ein[8 + j];
+        x += a.eix[8 + j];
+      }
+    it_in[tid] = g;
+    it_ix[tid] = x;
+  }
+  int64_t t_in = 0;  // element bits 0..7 come from the thread
+  int32_t t_ix = 0;
+  for (int j = 0; j < 8; ++j)
+    if ((tid >> j) & 1) {
+      t_in += a.ein[j];
+      t_ix += a.eix[j];
+    }
+  const int tcol = tid % NTC, trow = tid / NTC;
+  int64_t r_t = 0, c_t = 0;  // offsets of row 2*trow and column 2*tcol
+  for (int m = 0; m < K; ++m)
+    if (((2 * trow) >> m) & 1) r_t += a.boff[m];
+  for (int q = 0; q < W::LBN; ++q)
+    if (((2 * tcol) >> q) & 1) c_t += a.cout[q];
+  __syncthreads();
+
+  auto load_mat = [&](const float2* mat, int kc) {
+#pragma unroll
+    for (int i = 0; i < D * BK / 256; ++i) {
+      const int e = tid + 256 * i;
+      const int r = e / BK, kk = e % BK;
+      cp_async8(ms + r * LDM + kk, mat + (int64_t)r * D + kc + kk);
+    }
+  };
+
+  const uint64_t ntiles = (a.groups + BN - 1) >> W::LBN;
+  const uint64_t gmask = (uint64_t(1) << a.lgps) - 1;
+  int64_t loaded = -1;
+  for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const uint64_t g0 = t << W::LBN;
+    const uint64_t s0 = g0 >> a.lgps;
+    uint64_t gin = g0 & gmask;
+    for (int j = 0; j < a.nspos; ++j) gin = insert_zero(gin, a.spos[j]);
+    const float2* src = in + (int64_t)s0 * a.in_stride + gin;
+    float2* dst = out + (s0 << a.n) + gin;
+    const uint64_t left = a.groups - g0;
+    const int cv = left < (uint64_t)BN ? (int)left : BN;
+    const float2* mat = ops + (a.op_stride ? (int64_t)s0 * a.op_stride : 0);
+#pragma unroll 8
+    for (int i = 0; i < 32; ++i) {
+      const int32_t x = t_ix + it_ix[i];
+      const int b = x >> W::LBN, c = x & (BN - 1);
+      if (c < cv)
+        cp_async8(xs + b * BN + (c ^ ((b & SWM) << 1)),
+                  src + t_in + it_in[i]);
+    }
+    if constexpr (kResident) {
+      const int64_t id = a.op_stride ? (int64_t)s0 : 0;
+      if (id != loaded) {  // block-uniform
+        load_mat(mat, 0);
+        loaded = id;
+      }
+    } else {
+      load_mat(mat, 0);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+
+    float2 acc[TM][TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+      for (int j = 0; j < TN; ++j) acc[i][j] = make_float2(0.f, 0.f);
+    for (int kc = 0; kc < D; kc += BK) {
+      if (!kResident && kc) {
+        __syncthreads();  // the previous chunk is no longer read
+        load_mat(mat, kc);
+        cp_async_wait_all();
+        __syncthreads();
+      }
+#pragma unroll 2
+      for (int kk = 0; kk < BK; ++kk) {
+        const int b = kc + kk;
+        float2 av[TM], xv[TN];
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+          av[i] = ms[(2 * trow + 2 * NTR * (i >> 1) + (i & 1)) * LDM + kk];
+        const float2* xrow = xs + b * BN;
+        const int sw = (b & SWM) << 1;
+#pragma unroll
+        for (int j = 0; j < TN / 2; ++j) {
+          const float4 v = *reinterpret_cast<const float4*>(
+              xrow + ((2 * tcol + 2 * NTC * j) ^ sw));
+          xv[2 * j] = make_float2(v.x, v.y);
+          xv[2 * j + 1] = make_float2(v.z, v.w);
+        }
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+#pragma unroll
+          for (int j = 0; j < TN; ++j) acc[i][j] = cmad(av[i], xv[j], acc[i][j]);
+      }
+    }
+
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+      float2* drow = dst + r_t + a.rj[i] + c_t;
+#pragma unroll
+      for (int j = 0; j < TN / 2; ++j) {
+        const int c = 2 * tcol + 2 * NTC * j;
+        if (c >= cv) continue;
+        float2* p = drow + a.cj[2 * j];
+        if (a.vec) {
+          __stcs(reinterpret_cast<float4*>(p),
+                 make_float4(acc[i][2 * j].x, acc[i][2 * j].y,
+                             acc[i][2 * j + 1].x, acc[i][2 * j + 1].y));
+        } else {
+          __stcs(p, acc[i][2 * j]);
+          if (c + 1 < cv) __stcs(drow + a.cj[2 * j + 1], acc[i][2 * j + 1]);
+        }
+      }
+    }
+    __syncthreads();  // the tile and operator are no longer read
+  }
+}
+
+// Fills WideArgs for dense_wide_kernel<K> and launches it.
+template <int K>
+static int launch_wide(const float2* in, float2* out, const float2* ops,
+                       int n, int64_t num_states, int64_t in_stride,
+                       int64_t op_stride, const int* pos, cudaStream_t st) {
+  using W = WideCfg<K>;
+  WideArgs a{};
+  a.n = n;
+  a.lgps = n - K;
+  a.groups = (uint64_t)num_states << a.lgps;
+  a.in_stride = in_stride;
+  a.op_stride = op_stride;
+  a.nspos = K;
+  uint64_t tmask = 0;
+  for (int j = 0; j < K; ++j) {
+    a.spos[j] = pos[j];
+    tmask |= uint64_t(1) << pos[j];
+  }
+  std::sort(a.spos, a.spos + K);
+  for (int m = 0; m < K; ++m) a.boff[m] = int64_t(1) << pos[K - 1 - m];
+  // tile column bit q: a group bit inside the state (the q-th position that
+  // is not a target) or a state bit
+  int64_t cin[7] = {0};
+  int p = 0;
+  for (int q = 0; q < W::LBN; ++q) {
+    if (q < a.lgps) {
+      while ((tmask >> p) & 1) ++p;
+      cin[q] = a.cout[q] = int64_t(1) << p;
+      ++p;
+    } else {
+      cin[q] = in_stride << (q - a.lgps);
+      a.cout[q] = int64_t(1) << (n + q - a.lgps);
+    }
+  }
+  // element bits sorted by input address (broadcast bits, offset 0, last)
+  int64_t key[13];
+  int ne = 0;
+  for (int m = 0; m < K; ++m) {
+    a.ein[ne] = a.boff[m];
+    a.eix[ne++] = W::BN << m;
+  }
+  for (int q = 0; q < W::LBN; ++q) {
+    a.ein[ne] = cin[q];
+    a.eix[ne++] = 1 << q;
+  }
+  for (int j = 0; j < 13; ++j) key[j] = a.ein[j] ? a.ein[j] : INT64_MAX;
+  for (int i = 1; i < 13; ++i)
+    for (int j = i; j > 0 && key[j - 1] > key[j]; --j) {
+      std::swap(key[j - 1], key[j]);
+      std::swap(a.ein[j - 1], a.ein[j]);
+      std::swap(a.eix[j - 1], a.eix[j]);
+    }
+  for (int i = 0; i < W::TM; ++i) {
+    const int r = 2 * W::NTR * (i >> 1) + (i & 1);
+    int64_t o = 0;
+    for (int m = 0; m < K; ++m)
+      if ((r >> m) & 1) o += a.boff[m];
+    a.rj[i] = o;
+  }
+  for (int j = 0; j < W::TN; ++j) {
+    const int c = 2 * W::NTC * (j >> 1) + (j & 1);
+    int64_t o = 0;
+    for (int q = 0; q < W::LBN; ++q)
+      if ((c >> q) & 1) o += a.cout[q];
+    a.cj[j] = o;
+  }
+  a.vec = a.cout[0] == 1 && n >= 1 &&
+          reinterpret_cast<uintptr_t>(out) % 16 == 0;
+
+  // the shared-memory opt-in and the occupancy, once per device
+  static std::atomic<int> per_sm_of[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::atomic<int>& per_sm = per_sm_of[dev & 63];
+  int bps = per_sm.load(std::memory_order_relaxed);
+  if (bps == 0) {
+    cudaError_t e = cudaFuncSetAttribute(
+        dense_wide_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)W::SMEM);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &bps, dense_wide_kernel<K>, 256, W::SMEM);
+    if (e != cudaSuccess || bps < 1)
+      return set_error(GBSV_ERR_CUDA, "dense_wide_kernel<%d> setup: %s", K,
+                       cudaGetErrorString(e));
+    per_sm.store(bps, std::memory_order_relaxed);
+  }
+  const uint64_t ntiles = (a.groups + W::BN - 1) >> W::LBN;
+  uint64_t grid = (uint64_t)sm_count() * bps;
+  if (grid > ntiles) grid = ntiles;
+  dense_wide_kernel<K><<<(unsigned)grid, 256, W::SMEM, st>>>(in, out, ops, a);
+  return after_launch("dense_wide_kernel");
+}
+
+// Whether dense_wide_kernel takes this operator: complex64, 6 <= k <= 12,
+// one operator or a tile inside one state, and in place only over
+// contiguous states.
+static bool wide_applies(int dtype, int n, int k, int64_t num_states,
+                         int64_t in_stride, int64_t op_stride,
+                         bool in_place) {
+  if (dtype != GBSV_C64 || k < 6 || k > 12 || n < k) return false;
+  const int lbn = k == 6 ? 7 : 13 - k;
+  if (op_stride != 0 && n - k < lbn) return false;
+  if (in_place && num_states > 1 && in_stride != (int64_t(1) << n))
+    return false;
+  return true;
+}
+
+static int apply_wide(const void* in, void* out, int n, int64_t num_states,
+                      int64_t in_stride, const void* ops, int64_t op_stride,
+                      const int* pos, int k, cudaStream_t st) {
+  const float2* i = static_cast<const float2*>(in);
+  float2* o = static_cast<float2*>(out);
+  const float2* m = static_cast<const float2*>(ops);
+  switch (k) {
+    case 6: return launch_wide<6>(i, o, m, n, num_states, in_stride, op_stride, pos, st);
+    case 7: return launch_wide<7>(i, o, m, n, num_states, in_stride, op_stride, pos, st);
+    case 8: return launch_wide<8>(i, o, m, n, num_states, in_stride, op_stride, pos, st);
+    case 9: return launch_wide<9>(i, o, m, n, num_states, in_stride, op_stride, pos, st);
+    case 10: return launch_wide<10>(i, o, m, n, num_states, in_stride, op_stride, pos, st);
+    case 11: return launch_wide<11>(i, o, m, n, num_states, in_stride, op_stride, pos, st);
+    default: return launch_wide<12>(i, o, m, n, num_states, in_stride, op_stride, pos, st);
+  }
+}
+
 static int apply_generic(const void* in, void* out, int dtype, int n,
                          int64_t num_states, int64_t in_stride,
                          const void* ops, int64_t op_stride, const int* pos,
                          int k, cudaStream_t st) {
+  if (wide_applies(dtype, n, k, num_states, in_stride, op_stride, in == out))
+    return apply_wide(in, out, n, num_states, in_stride, ops, op_stride, pos,
+                      k, st);
   GenericArgs a{};
   a.total = (uint64_t)num_states << n;
   a.n = n;

@@ -146,6 +146,14 @@ __device__ __forceinline__ void cp_async16(Cx<R>* smem, const Cx<R>* gmem) {
                : "memory");
 }
 
+// 8-byte asynchronous global -> shared copy (cp.async.ca, through L1).
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s),
+               "l"(gmem)
+               : "memory");
+}
+
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }

@@ -840,8 +840,9 @@ class Program:
         else:
             _, mat, qubits = op
             op_stride = 0 if mat.dim() == 2 else mat.shape[-1] ** 2
-            wide = (cur.data_ptr() == out.data_ptr() and len(qubits) >
-                    _core.max_inplace_qubits(self.dtype))
+            wide = (cur.data_ptr() == out.data_ptr() and not
+                    _core.inplace_ok(self.dtype, len(qubits), self.n,
+                                     op_stride != 0))
             dst = torch.empty_like(out) if wide else out
             rc = L.gbsv_apply_operator(
                 cur.data_ptr(), dst.data_ptr(), self.code, self.n, B, N,

@@ -250,8 +250,8 @@ def apply_operator_(operator: torch.Tensor, qubits: Iterable[int],
         raise ValueError("apply_operator_ cannot broadcast an unbatched "
                          "state over an operator batch")
     if plan.num_states:
-        wide = k > _core.max_inplace_qubits(state.dtype)
-        if wide:  # the wide-operator kernel is not in place
+        wide = not _core.inplace_ok(state.dtype, k, n, plan.op_stride != 0)
+        if wide:  # this operator is not applied in place
             out = torch.empty_like(state)
             _launch_apply(plan.ops, plan.op_stride, state, 2 ** n, out, n,
                           qubits, plan.num_states)
