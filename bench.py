@@ -69,6 +69,17 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def sm_max_mhz():
+    """Maximum SM clock of the GB300s (MEASURED_PEAKS.json; 2070 MHz
+    nominal otherwise)."""
+    f = REPO / "MEASURED_PEAKS.json"
+    if f.exists():
+        v = json.loads(f.read_text()).get("sm_max_mhz")
+        if v:
+            return float(v)
+    return 2070.0
+
+
 # DRAM bytes (read + write) of one dense_chunk_kernel launch on a 30-qubit
 # complex64 state: ncu dram__bytes_read.sum + dram__bytes_write.sum of a
 # 26-qubit capture, scaled by 16 (traffic is proportional to the state; a
@@ -543,6 +554,63 @@ def bench_next_rows(dev, n=30):
         torch.cuda.empty_cache()
     return {"workload": f"{n}-qubit complex64 state ({8 * 2 ** n / 2 ** 30:g} GiB), functional API",
             "peak_GBs": peak, "ops": out}
+
+
+# ------------------------------------------ operators on 6-12 qubits ------
+def bench_wide_ops(dev, n=30):
+    """Dense 6- and 8-qubit operators (random unitaries) on a 30-qubit
+    complex64 state (8 GiB), in place through apply_operator_ and (k = 6)
+    through the functional apply_operator.  Targets on the high qubits
+    (0..k-1: the state's most significant bits) and on the low ones
+    (n-k..n-1: bit 0 among the targets).  Each output amplitude is a
+    2^k-term complex dot product: 8 * 2^k FP32 flops per amplitude, so the
+    bound is the FP32 pipe (SMs x 128 lanes x 2 flops x clock), not HBM;
+    both fractions are reported."""
+    import numpy as np
+    import torch
+    import qcware_unitair_gb300 as ug
+    N = 2 ** n
+    g = torch.Generator(device=dev)
+    g.manual_seed(9)
+    psi = torch.randn(N, dtype=torch.complex64, device=dev, generator=g)
+    psi /= torch.linalg.vector_norm(psi)
+    peak = peaks()[0]
+    props = torch.cuda.get_device_properties(dev)
+    sm_mhz = sm_max_mhz()
+    fp32_peak = props.multi_processor_count * 128 * 2 * sm_mhz / 1e6  # TF/s
+    rng = np.random.default_rng(4)
+    ops = {}
+    for k in (6, 8):
+        a = rng.standard_normal((2 ** k, 2 ** k)) + \
+            1j * rng.standard_normal((2 ** k, 2 ** k))
+        q, r = np.linalg.qr(a)
+        ops[k] = torch.from_numpy(q * (np.diag(r) / np.abs(np.diag(r)))).to(
+            dev, torch.complex64)
+    cases = []
+    for k in (6, 8):
+        for where, qs in (("high", list(range(k))),
+                          ("low", list(range(n - k, n)))):
+            cases.append((f"apply_operator_({k} qubits, {where})", k,
+                          lambda k=k, qs=qs: ug.apply_operator_(ops[k], qs,
+                                                                psi)))
+    cases.append(("apply_operator(6 qubits, high)", 6,
+                  lambda: ug.apply_operator(ops[6], list(range(6)), psi)))
+    out = {}
+    for name, k, fn in cases:
+        ms = _cuda_time(fn, 3)
+        gbs = 16 * N / (ms / 1e3) / 1e9
+        tfl = 8 * N * 2 ** k / (ms / 1e3) / 1e12
+        out[name] = {"ms": round(ms, 3), "GB_s": round(gbs, 1),
+                     "frac_of_copy_peak": round(gbs / peak, 3),
+                     "fp32_TFLOPs": round(tfl, 1),
+                     "frac_of_fp32_peak": round(tfl / fp32_peak, 3)}
+        torch.cuda.empty_cache()
+    nrm = float(ug.norm_squared(psi))
+    return {"workload": f"{n}-qubit complex64 state ({8 * N / 2 ** 30:g} GiB), "
+                        "random unitaries; in place repeats the operator",
+            "peak_GBs": peak, "fp32_peak_TFLOPs": round(fp32_peak, 1),
+            "fp32_peak_basis": "SMs x 128 FP32 lanes x 2 x max SM clock",
+            "norm_after": round(nrm, 6), "ops": out}
 
 
 # ------------------------------------------------- C1 in complex128 -------
@@ -1249,6 +1317,10 @@ def run_gpu(args, ws, rank, local):
         result["c2_16q_x4096"] = bench_c2(dev)
         result["path_rows_30q"] = bench_path_rows(dev)
         result["next_rows_30q"] = bench_next_rows(dev)
+        try:
+            result["wide_ops_30q"] = bench_wide_ops(dev)
+        except Exception as e:  # an extra never loses the line
+            result["wide_ops_30q"] = {"error": f"{type(e).__name__}: {e}"[:300]}
         result["adjoint"] = bench_adjoint(dev)
         result["serving"] = bench_serving(dev)
         for key, fn in (("serving_10_28", bench_serving_full_range),

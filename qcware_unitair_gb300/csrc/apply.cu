@@ -1237,11 +1237,19 @@ static int apply_small(const void* in, void* out, int dtype, int n,
 // streamed through shared memory in chunks of BK columns (k = 6 keeps the
 // whole 64 x 64 operator resident).  Each thread accumulates TM x TN = 32
 // outputs in registers; per k-step it reads TM operator entries (two thread
-// rows per warp: broadcasts) and TN/2 16-byte amplitude pairs.  Every output
-// sums over the operator's columns in order with the fused multiply-adds of
-// dense_generic_kernel, so both kernels give the same bits.  A tile is read
-// completely before any of it is written, and tiles are disjoint, so in
-// place is safe.
+// rows per warp: broadcasts) and TN/2 16-byte amplitude pairs.  Tile rows
+// are XOR-swizzled by 16-byte pairs (row & 15) so that copies of low-target
+// tiles spread over the banks; k = 6..8 walk rows in unrolled blocks of 16,
+// where the swizzle is a constant of each step and every shared load has an
+// immediate offset (the FP32 pipe is then the bound, not integer address
+// work).  Amplitudes are copied in by cp.async in input-address order; the
+// outputs are stored straight from registers when a thread's column pairs
+// are adjacent in memory (target bit 0 free), else staged through shared
+// memory and written in the same address order (coalesced either way).
+// Every output sums over the operator's columns in order with the fused
+// multiply-adds of dense_generic_kernel, so both kernels give the same
+// bits.  A tile is read completely before any of it is written, and tiles
+// are disjoint, so in place is safe.
 template <int K>
 struct WideCfg {
   static constexpr int D = 1 << K;
@@ -1272,6 +1280,7 @@ struct WideArgs {
   // the 13 bits of a tile element index (row b, column c), lowest input
   // address first: input address offset and shared index (b * BN + c)
   int64_t ein[13];
+  int64_t eout[13];  // output address offset of the same bits
   int32_t eix[13];
   int64_t rj[16];    // offs(2 * NTR * (i >> 1) + (i & 1)), i < TM
   int64_t cj[8];     // output offset of column 2 * NTC * (j >> 1) + (j & 1)
@@ -1288,25 +1297,28 @@ __global__ void __launch_bounds__(256, K <= 10 ? 2 : 1)
   extern __shared__ __align__(16) float2 wsm[];
   float2* xs = wsm;           // [D][BN] the tile, columns XOR-swizzled
   float2* ms = wsm + D * BN;  // [D][LDM] columns kc .. kc + BK - 1
-  __shared__ int64_t it_in[32];
+  __shared__ int64_t it_in[32], it_out[32];
   __shared__ int32_t it_ix[32];
   const int tid = threadIdx.x;
   if (tid < 32) {  // element bits 8..12 come from the copy iteration
-    int64_t g = 0;
+    int64_t g = 0, o = 0;
     int32_t x = 0;
     for (int j = 0; j < 5; ++j)
       if ((tid >> j) & 1) {
         g += a.ein[8 + j];
+        o += a.eout[8 + j];
         x += a.eix[8 + j];
       }
     it_in[tid] = g;
+    it_out[tid] = o;
     it_ix[tid] = x;
   }
-  int64_t t_in = 0;  // element bits 0..7 come from the thread
+  int64_t t_in = 0, t_out = 0;  // element bits 0..7 come from the thread
   int32_t t_ix = 0;
   for (int j = 0; j < 8; ++j)
     if ((tid >> j) & 1) {
       t_in += a.ein[j];
+      t_out += a.eout[j];
       t_ix += a.eix[j];
     }
   const int tcol = tid % NTC, trow = tid / NTC;
@@ -1371,6 +1383,36 @@ __global__ void __launch_bounds__(256, K <= 10 ? 2 : 1)
         cp_async_wait_all();
         __syncthreads();
       }
+      if constexpr (BK >= 16 && SWM == 15) {
+        // blocks of 16 rows: the swizzle of row kc + k16 + u is 2u, a
+        // constant of the unrolled step
+        for (int k16 = 0; k16 < BK; k16 += 16) {
+          const float2* xblk = xs + (kc + k16) * BN;
+          const float2* mblk = ms + (2 * trow) * LDM + k16;
+#pragma unroll
+          for (int u = 0; u < 16; ++u) {
+            float2 av[TM], xv[TN];
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+              av[i] = mblk[(2 * NTR * (i >> 1) + (i & 1)) * LDM + u];
+            const float2* xrow = xblk + u * BN;
+            const int c0 = (2 * tcol) ^ (2 * u);
+#pragma unroll
+            for (int j = 0; j < TN / 2; ++j) {
+              const float4 v = *reinterpret_cast<const float4*>(
+                  xrow + (c0 ^ (2 * NTC * j)));
+              xv[2 * j] = make_float2(v.x, v.y);
+              xv[2 * j + 1] = make_float2(v.z, v.w);
+            }
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+              for (int j = 0; j < TN; ++j)
+                acc[i][j] = cmad(av[i], xv[j], acc[i][j]);
+          }
+        }
+        continue;
+      }
 #pragma unroll 2
       for (int kk = 0; kk < BK; ++kk) {
         const int b = kc + kk;
@@ -1394,6 +1436,31 @@ __global__ void __launch_bounds__(256, K <= 10 ? 2 : 1)
       }
     }
 
+    if (!a.vec) {
+      // outputs through shared memory, then out in input-address order
+      __syncthreads();  // the tile is no longer read
+#pragma unroll
+      for (int i = 0; i < TM; ++i) {
+        const int row = 2 * trow + 2 * NTR * (i >> 1) + (i & 1);
+        float2* srow = xs + row * BN;
+        const int sw = (row & SWM) << 1;
+#pragma unroll
+        for (int j = 0; j < TN / 2; ++j)
+          *reinterpret_cast<float4*>(srow + ((2 * tcol + 2 * NTC * j) ^ sw)) =
+              make_float4(acc[i][2 * j].x, acc[i][2 * j].y,
+                          acc[i][2 * j + 1].x, acc[i][2 * j + 1].y);
+      }
+      __syncthreads();
+#pragma unroll 8
+      for (int i = 0; i < 32; ++i) {
+        const int32_t x = t_ix + it_ix[i];
+        const int b = x >> W::LBN, c = x & (BN - 1);
+        if (c < cv)
+          __stcs(dst + t_out + it_out[i], xs[b * BN + (c ^ ((b & SWM) << 1))]);
+      }
+      __syncthreads();  // the tile is no longer read
+      continue;
+    }
 #pragma unroll
     for (int i = 0; i < TM; ++i) {
       float2* drow = dst + r_t + a.rj[i] + c_t;
@@ -1455,10 +1522,12 @@ static int launch_wide(const float2* in, float2* out, const float2* ops,
   int ne = 0;
   for (int m = 0; m < K; ++m) {
     a.ein[ne] = a.boff[m];
+    a.eout[ne] = a.boff[m];
     a.eix[ne++] = W::BN << m;
   }
   for (int q = 0; q < W::LBN; ++q) {
     a.ein[ne] = cin[q];
+    a.eout[ne] = a.cout[q];
     a.eix[ne++] = 1 << q;
   }
   for (int j = 0; j < 13; ++j) key[j] = a.ein[j] ? a.ein[j] : INT64_MAX;
@@ -1466,6 +1535,7 @@ static int launch_wide(const float2* in, float2* out, const float2* ops,
     for (int j = i; j > 0 && key[j - 1] > key[j]; --j) {
       std::swap(key[j - 1], key[j]);
       std::swap(a.ein[j - 1], a.ein[j]);
+      std::swap(a.eout[j - 1], a.eout[j]);
       std::swap(a.eix[j - 1], a.eix[j]);
     }
   for (int i = 0; i < W::TM; ++i) {
