@@ -786,6 +786,9 @@ def parse_cpulist(txt: str) -> set:
 #   serve NUM            the serving trace (150/s, 10-22 qubits) on the server
 #                        after a 16-request warm-up, with host time per path
 #   kinds N              one plain complex128 gate of each kind, 10 launches
+#   wide N K [low]       one dense K-qubit unitary (numpy seed K) in place on
+#                        an N-qubit complex64 state, targets 0..K-1 (or
+#                        N-K..N-1 with "low")
 def _wl_timed(fn):
     import torch
     fn()
@@ -987,6 +990,27 @@ def wl_phase128(n: int = 28) -> None:
     ug.set_complex128_arithmetic("pairs")
 
 
+def wl_wide(n: int = 26, k: int = 6, where: str = "high") -> None:
+    """One dense k-qubit unitary applied in place to an n-qubit complex64
+    state (the wide-operator tile kernel)."""
+    import numpy as np
+    import torch
+    import qcware_unitair_gb300 as ug
+    dev = torch.device("cuda")
+    g = torch.Generator(device=dev)
+    g.manual_seed(0)
+    psi = torch.randn(2 ** n, dtype=torch.complex64, device=dev, generator=g)
+    rng = np.random.default_rng(k)
+    q, r = np.linalg.qr(rng.standard_normal((2 ** k, 2 ** k)) +
+                        1j * rng.standard_normal((2 ** k, 2 ** k)))
+    op = torch.from_numpy(q * (np.diag(r) / np.abs(np.diag(r)))).to(
+        dev, torch.complex64)
+    qs = list(range(n - k, n)) if where == "low" else list(range(k))
+    ms = _wl_timed(lambda: ug.apply_operator_(op, qs, psi))
+    print(f"wide n={n} k={k} {where}: {ms:.3f} ms "
+          f"{8 * 2 ** n * 2 ** k / ms / 1e9:.1f} FP32 TFLOP/s")
+
+
 def run_workload(argv):
     import torch  # noqa: F401  (CUDA initialised before the workload)
     what, args = argv[0], argv[1:]
@@ -1012,6 +1036,10 @@ def run_workload(argv):
     elif what == "kinds":
         wl_kinds(int(args[0]) if args else 28,
                  args[1] if len(args) > 1 else "pairs")
+    elif what == "wide":
+        wl_wide(int(args[0]) if args else 26,
+                int(args[1]) if len(args) > 1 else 6,
+                args[2] if len(args) > 2 else "high")
     else:
         raise SystemExit(f"unknown workload {what}")
 
