@@ -97,3 +97,43 @@ def test_complex128_arithmetic_switch_without_gpu(lib_built):
             ug.set_complex128_arithmetic("double")
     finally:
         L.gbsv_set_c128_arith(prev)
+
+
+def test_inplace_rule_matches_the_library(lib_built):
+    """_core.inplace_ok (which tells callers when to go through a
+    temporary) agrees with gbsv_apply_operator: every in-place request it
+    marks unsupported is refused with GBSV_ERR_UNSUPPORTED before any CUDA
+    call (dummy pointers, never dereferenced).  Supported requests would
+    launch kernels and are not called here; with a GPU present the test
+    is skipped, so that a disagreement can never reach a launch."""
+    import torch
+    from qcware_unitair_gb300 import _core
+    if torch.cuda.is_available():
+        pytest.skip("dummy pointers: run without a GPU")
+    L = _lib.load()
+    p = 4096  # dummy device address
+    for dtype, code in ((torch.complex64, _lib.C64),
+                        (torch.complex128, _lib.C128)):
+        for k in range(3, 13):
+            for n in (k, k + 1, k + 3, k + 8):
+                for per_state in (False, True):
+                    if _core.inplace_ok(dtype, k, n, per_state):
+                        continue
+                    q = _lib.qubit_array(list(range(k)))
+                    rc = L.gbsv_apply_operator(
+                        p, p, code, n, 2, 2 ** n, p,
+                        4 ** k if per_state else 0, q, k, None)
+                    assert rc == _lib.GBSV_ERR_UNSUPPORTED, (dtype, k, n,
+                                                             per_state)
+                    assert b"in place" in L.gbsv_last_error()
+    # complex64 wide operators: in place for shared operators at any size,
+    # per-state ones once a state holds a whole tile of groups
+    assert _core.inplace_ok(torch.complex64, 12, 12)
+    assert not _core.inplace_ok(torch.complex64, 6, 12, True)
+    assert _core.inplace_ok(torch.complex64, 6, 13, True)
+    assert _core.inplace_ok(torch.complex64, 12, 13, True)
+    assert not _core.inplace_ok(torch.complex128, 5, 20)
+    # a strided batch in place is refused even for a shared operator
+    q = _lib.qubit_array(list(range(7)))
+    assert L.gbsv_apply_operator(p, p, _lib.C64, 9, 3, 2 ** 9 + 6, p, 0, q,
+                                 7, None) == _lib.GBSV_ERR_UNSUPPORTED
