@@ -329,6 +329,25 @@ def main(ref_root: str) -> None:
                        "state_shape": list(sshape), "qubits": qs,
                        "op_dtype": odt, "state_dtype": sdt, **result})
 
+    # ---- operators on 6-8 qubits (drawn last: earlier cases keep their
+    # random inputs) -----------------------------------------------------
+    wide_specs = [
+        # (operator batch, state batch, n, qubits, dtype)
+        ((), (2,), 8, [5, 0, 7, 2, 6, 3], torch.complex64),   # bit 0 targeted
+        ((), (3,), 7, [6, 1, 4, 0, 3, 5], torch.complex128),
+        ((), (3,), 7, [3, 6, 0, 5, 1, 4, 2], torch.complex64),  # n == k
+        ((), (), 10, [0, 2, 4, 6, 8, 1, 3, 5], torch.complex64),
+        ((3,), (), 9, [8, 1, 4, 6, 2, 0], torch.complex64),   # state broadcast
+    ]
+    for j, (ob, sb, n, qs, dtype) in enumerate(wide_specs):
+        k = len(qs)
+        op = cplx(ob + (2 ** k, 2 ** k), dtype) / 2 ** (k / 2)
+        st = cplx(sb + (2 ** n,), dtype)
+        name = f"apply_wide_{j}"
+        put(name, op=op, state=st, out=apply_operator(op, qs, st))
+        cases.append({"name": name, "kind": "apply", "qubits": qs, "n": n,
+                      "k": k, "dtype": str(dtype)})
+
     np.savez_compressed(HERE / "golden.npz", **arrays)
     meta = {"reference": "unitair 0.3.0 (setup.cfg:3)",
             "torch": torch.__version__, "cases": cases, "errors": errors}
