@@ -347,6 +347,17 @@ def main(ref_root: str) -> None:
         put(name, op=op, state=st, out=apply_operator(op, qs, st))
         cases.append({"name": name, "kind": "apply", "qubits": qs, "n": n,
                       "k": k, "dtype": str(dtype)})
+    # ---- 5-qubit operators (drawn after the wide cases) -----------------
+    for j, (ob, sb, n, qs, dtype) in enumerate([
+            ((2,), (2,), 7, [4, 6, 0, 2, 5], torch.complex64),
+            ((), (3,), 6, [5, 3, 1, 0, 2], torch.complex128)]):
+        k = len(qs)
+        op = cplx(ob + (2 ** k, 2 ** k), dtype) / 2 ** (k / 2)
+        st = cplx(sb + (2 ** n,), dtype)
+        name = f"apply_k5_{j}"
+        put(name, op=op, state=st, out=apply_operator(op, qs, st))
+        cases.append({"name": name, "kind": "apply", "qubits": qs, "n": n,
+                      "k": k, "dtype": str(dtype)})
 
     np.savez_compressed(HERE / "golden.npz", **arrays)
     meta = {"reference": "unitair 0.3.0 (setup.cfg:3)",
