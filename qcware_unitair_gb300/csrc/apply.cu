@@ -1253,10 +1253,10 @@ static int apply_small(const void* in, void* out, int dtype, int n,
 template <int K>
 struct WideCfg {
   static constexpr int D = 1 << K;
-  static constexpr int LBN = K == 6 ? 7 : 13 - K;  // log2 groups per tile
+  static constexpr int LBN = 13 - K;               // log2 groups per tile
   static constexpr int BN = 1 << LBN;
-  static constexpr int BK = 4096 >> K;             // columns per chunk
-  static constexpr int TN = K == 6 ? 8 : (K == 12 ? 2 : 4);
+  static constexpr int BK = (4096 >> K) < D ? (4096 >> K) : D;  // chunk
+  static constexpr int TN = K <= 6 ? 8 : (K == 12 ? 2 : 4);
   static constexpr int TM = 32 / TN;
   static constexpr int NTC = BN / TN;              // thread columns
   static constexpr int NTR = 256 / NTC;            // thread rows
@@ -1276,7 +1276,7 @@ struct WideArgs {
   int64_t op_stride;
   int spos[GBSV_MAX_DENSE_QUBITS];     // target positions, ascending
   int64_t boff[GBSV_MAX_DENSE_QUBITS]; // address offset of matrix bit m
-  int64_t cout[7];   // output address offset of tile column bit q
+  int64_t cout[9];   // output address offset of tile column bit q
   // the 13 bits of a tile element index (row b, column c), lowest input
   // address first: input address offset and shared index (b * BN + c)
   int64_t ein[13];
@@ -1505,7 +1505,7 @@ static int launch_wide(const float2* in, float2* out, const float2* ops,
   for (int m = 0; m < K; ++m) a.boff[m] = int64_t(1) << pos[K - 1 - m];
   // tile column bit q: a group bit inside the state (the q-th position that
   // is not a target) or a state bit
-  int64_t cin[7] = {0};
+  int64_t cin[9] = {0};
   int p = 0;
   for (int q = 0; q < W::LBN; ++q) {
     if (q < a.lgps) {
@@ -1580,14 +1580,24 @@ static int launch_wide(const float2* in, float2* out, const float2* ops,
   return after_launch("dense_wide_kernel");
 }
 
-// Whether dense_wide_kernel takes this operator: complex64, 6 <= k <= 12,
+// Whether dense_wide_kernel takes this operator: complex64, 4 <= k <= 12,
 // one operator or a tile inside one state, and in place only over
-// contiguous states.
+// contiguous states.  Below 6 qubits the group kernel is the alternative:
+// the tile kernel takes every 5-qubit operator (the group kernel's 32
+// amplitudes per thread leave it at half the tile kernel's rate) and
+// 4-qubit operators with a target among the three lowest bits (groups of
+// contiguous amplitudes, where consecutive threads of the group kernel
+// read lines 128 bytes or more apart).
 static bool wide_applies(int dtype, int n, int k, int64_t num_states,
                          int64_t in_stride, int64_t op_stride,
-                         bool in_place) {
-  if (dtype != GBSV_C64 || k < 6 || k > 12 || n < k) return false;
-  const int lbn = k == 6 ? 7 : 13 - k;
+                         bool in_place, const int* pos) {
+  if (dtype != GBSV_C64 || k < 4 || k > 12 || n < k) return false;
+  if (k == 4) {
+    int lowest = 64;
+    for (int j = 0; j < k; ++j) lowest = pos[j] < lowest ? pos[j] : lowest;
+    if (lowest >= 3) return false;
+  }
+  const int lbn = 13 - k;
   if (op_stride != 0 && n - k < lbn) return false;
   if (in_place && num_states > 1 && in_stride != (int64_t(1) << n))
     return false;
@@ -1601,6 +1611,8 @@ static int apply_wide(const void* in, void* out, int n, int64_t num_states,
   float2* o = static_cast<float2*>(out);
   const float2* m = static_cast<const float2*>(ops);
   switch (k) {
+    case 4: return launch_wide<4>(i, o, m, n, num_states, in_stride, op_stride, pos, st);
+    case 5: return launch_wide<5>(i, o, m, n, num_states, in_stride, op_stride, pos, st);
     case 6: return launch_wide<6>(i, o, m, n, num_states, in_stride, op_stride, pos, st);
     case 7: return launch_wide<7>(i, o, m, n, num_states, in_stride, op_stride, pos, st);
     case 8: return launch_wide<8>(i, o, m, n, num_states, in_stride, op_stride, pos, st);
@@ -1615,7 +1627,8 @@ static int apply_generic(const void* in, void* out, int dtype, int n,
                          int64_t num_states, int64_t in_stride,
                          const void* ops, int64_t op_stride, const int* pos,
                          int k, cudaStream_t st) {
-  if (wide_applies(dtype, n, k, num_states, in_stride, op_stride, in == out))
+  if (wide_applies(dtype, n, k, num_states, in_stride, op_stride, in == out,
+                   pos))
     return apply_wide(in, out, n, num_states, in_stride, ops, op_stride, pos,
                       k, st);
   GenericArgs a{};
