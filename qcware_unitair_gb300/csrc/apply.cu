@@ -909,7 +909,9 @@ __global__ void __launch_bounds__(256)
 
 // k = 3..5 target qubits: one thread per group of 2^k amplitudes (two
 // groups when one matrix serves all states and both fit in 256 bytes of
-// registers).  The thread reads its group once (consecutive threads take consecutive groups,
+// registers).  complex64 5-qubit operators, and 4-qubit ones with a target
+// among the three lowest bits, go to dense_wide_kernel instead
+// (wide_applies); this kernel remains their in-place fallback.  The thread reads its group once (consecutive threads take consecutive groups,
 // so every load instruction of a warp is contiguous when bit 0 is not a
 // target), multiplies by the matrix (in shared memory when one matrix
 // serves all states) and writes the group; in place is safe.
@@ -1231,15 +1233,16 @@ static int apply_small(const void* in, void* out, int dtype, int n,
 }
 
 // ------------------------------------------------ wide operators (c64) ----
-// k = 6..12 target qubits, complex64: a CTA holds a "tile" of BN groups (all
-// 2^k amplitudes of each, 8192 amplitudes = 64 KB) in shared memory and
+// k = 4..12 target qubits, complex64 (k = 4, 5 where the group kernel is
+// slower, see wide_applies): a CTA holds a "tile" of BN = 2^(13-k) groups
+// (all 2^k amplitudes of each, 8192 amplitudes = 64 KB) in shared memory and
 // computes the D x BN output tile as a complex matrix product, the operator
-// streamed through shared memory in chunks of BK columns (k = 6 keeps the
-// whole 64 x 64 operator resident).  Each thread accumulates TM x TN = 32
-// outputs in registers; per k-step it reads TM operator entries (two thread
+// streamed through shared memory in chunks of BK columns (k <= 6 keeps the
+// whole operator resident).  Each thread accumulates TM x TN = 32 outputs
+// in registers; per k-step it reads TM operator entries (at most two thread
 // rows per warp: broadcasts) and TN/2 16-byte amplitude pairs.  Tile rows
 // are XOR-swizzled by 16-byte pairs (row & 15) so that copies of low-target
-// tiles spread over the banks; k = 6..8 walk rows in unrolled blocks of 16,
+// tiles spread over the banks; k = 4..8 walk rows in unrolled blocks of 16,
 // where the swizzle is a constant of each step and every shared load has an
 // immediate offset (the FP32 pipe is then the bound, not integer address
 // work).  Amplitudes are copied in by cp.async in input-address order; the
@@ -1411,28 +1414,28 @@ __global__ void __launch_bounds__(256, K <= 10 ? 2 : 1)
                 acc[i][j] = cmad(av[i], xv[j], acc[i][j]);
           }
         }
-        continue;
-      }
+      } else {
 #pragma unroll 2
-      for (int kk = 0; kk < BK; ++kk) {
-        const int b = kc + kk;
-        float2 av[TM], xv[TN];
+        for (int kk = 0; kk < BK; ++kk) {
+          const int b = kc + kk;
+          float2 av[TM], xv[TN];
 #pragma unroll
-        for (int i = 0; i < TM; ++i)
-          av[i] = ms[(2 * trow + 2 * NTR * (i >> 1) + (i & 1)) * LDM + kk];
-        const float2* xrow = xs + b * BN;
-        const int sw = (b & SWM) << 1;
+          for (int i = 0; i < TM; ++i)
+            av[i] = ms[(2 * trow + 2 * NTR * (i >> 1) + (i & 1)) * LDM + kk];
+          const float2* xrow = xs + b * BN;
+          const int sw = (b & SWM) << 1;
 #pragma unroll
-        for (int j = 0; j < TN / 2; ++j) {
-          const float4 v = *reinterpret_cast<const float4*>(
-              xrow + ((2 * tcol + 2 * NTC * j) ^ sw));
-          xv[2 * j] = make_float2(v.x, v.y);
-          xv[2 * j + 1] = make_float2(v.z, v.w);
+          for (int j = 0; j < TN / 2; ++j) {
+            const float4 v = *reinterpret_cast<const float4*>(
+                xrow + ((2 * tcol + 2 * NTC * j) ^ sw));
+            xv[2 * j] = make_float2(v.x, v.y);
+            xv[2 * j + 1] = make_float2(v.z, v.w);
+          }
+#pragma unroll
+          for (int i = 0; i < TM; ++i)
+#pragma unroll
+            for (int j = 0; j < TN; ++j) acc[i][j] = cmad(av[i], xv[j], acc[i][j]);
         }
-#pragma unroll
-        for (int i = 0; i < TM; ++i)
-#pragma unroll
-          for (int j = 0; j < TN; ++j) acc[i][j] = cmad(av[i], xv[j], acc[i][j]);
       }
     }
 
