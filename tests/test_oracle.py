@@ -125,3 +125,21 @@ def test_oracle_rejects_bad_qubits(oracle):
         oracle.apply_operator(np.eye(2), [3], np.ones(8))
     with pytest.raises(ValueError):
         oracle.apply_operator(np.eye(4), [1, 1], np.ones(8))
+
+
+@pytest.mark.parametrize("k", [9, 10, 11, 12])
+def test_oracle_wide_operators_match_numpy(oracle, k):
+    """Operators on 9-12 qubits (too large for golden files): the C oracle
+    against the independent einsum restatement, shared and per-state
+    operators, targets in a scrambled order."""
+    rng = np.random.default_rng(500 + k)
+    n = k + 1
+    qubits = [int(q) for q in rng.permutation(n)[:k]]
+    st = rng.standard_normal((2, 2 ** n)) + 1j * rng.standard_normal((2, 2 ** n))
+    for shape in ((2 ** k, 2 ** k), (2, 2 ** k, 2 ** k)):
+        op = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)) \
+            / 2 ** (k / 2)
+        got = oracle.apply_operator(op, qubits, st)
+        ref = oracle.apply_operator_numpy(op, qubits, st)
+        scale = max(1.0, np.abs(ref).max())
+        np.testing.assert_allclose(got, ref, atol=1e-12 * scale, rtol=0)
